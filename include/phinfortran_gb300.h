@@ -1,0 +1,121 @@
+/*
+ * phinfortran_gb300.h -- C ABI of the GB300 NEGF transport engine.
+ *
+ * Drop-in for the per-(ie,ik) hot loop of KitchenSong/phinfortran's tdb
+ * transport branch (negf/phinfortran.f90:1188-1251).  The Fortran driver
+ * keeps its input readers, grids and output writers and calls these
+ * functions through iso_c_binding.
+ *
+ * Conventions (those of the reference's arrays):
+ *  - every matrix is complex(kind=8), column-major, passed as double* to
+ *    interleaved (re, im) pairs; element (r, c) of an m-row block sits at
+ *    [2*(r + c*m)] / [2*(r + c*m) + 1];
+ *  - per-q block sets are stacked: HL[q][nl*nl], Hd[q][L][n*n], ...;
+ *  - "tdb" block names follow negf/dyn.f90:1482-2080:
+ *      HL  = Haml   left lead cell onsite        (nl x nl)
+ *      HLv = Hamlv  H_{-1,0}  lead cell coupling (nl x nl)
+ *      HR  = Hamr   right lead cell onsite       (nr x nr)
+ *      HRv = Hamrv  H_{N+2,N+1}                  (nr x nr)
+ *      Hd  = Hamd   device layer onsite          (L blocks, n x n)
+ *      Hdv = Hamdv  H_{i,i+1}                    (L-1 blocks, n x n)
+ *      Hld = Hamld  H_{0,1}                      (nl x n)
+ *      Hrd = Hamrd  H_{N+1,N}                    (nr x n)
+ *  - energies are the reference's Egrid values (omega^2 in THz^2 for the
+ *    phonon driver, E for the electron driver);
+ *  - lead broadening eps = E*eta + eta0 (negf/surface.f90:479); the device
+ *    uses E + i*dev_factor*eps (dev_factor = 10 reproduces
+ *    negf/lesser.f90:556, 1 reproduces tb/device.f90:390 with eta = 0,
+ *    eta0 = the tb eta);
+ *  - transmissions below 1e-60 are returned as 0 (negf/lesser.f90:795-800)
+ *    and points flagged in zero_flag return 0 (the ie == 1 rule,
+ *    negf/lesser.f90:802-807).
+ *
+ * Return codes: PF_SUCCESS, a negative PF_ERR_* for argument / CUDA
+ * errors, or PF_ERR_POINT when any point's status word is nonzero (the
+ * reference would `stop` there: util.f90:29-66).  pf_last_error() gives a
+ * message.  Per-point status bits: 1 singular block, 2 non-finite value,
+ * 4 decimation reached max_iter (the reference loop is unbounded,
+ * negf/surface.f90:488).
+ */
+#ifndef PHINFORTRAN_GB300_H
+#define PHINFORTRAN_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PF_ABI_VERSION 1
+
+#define PF_SUCCESS 0
+#define PF_ERR_ARG (-1)
+#define PF_ERR_CUDA (-2)
+#define PF_ERR_SIZE (-3)
+#define PF_ERR_POINT (-4)
+
+/* Largest block dimension (n, nl, nr) of the shared-memory resident kernel. */
+#define PF_NMAX_RESIDENT 48
+
+/* Message for the last error on the calling thread. */
+const char* pf_last_error(void);
+
+/* ABI version (PF_ABI_VERSION of the built library). */
+int pf_version(void);
+
+/*
+ * Fused transport for a batch of (omega, q) points, device pointers.
+ *
+ * Replaces, per point p = (ie, ik):
+ *   surface_green_tdb_mpi(ie, ik, ...)   negf/surface.f90:344-383
+ *     (left advanced and right retarded decimations, Sigma, Gamma)
+ *   get_G_full_tdb_mpi(ie, ik, ...)      negf/lesser.f90:100-157
+ *     (left-to-right sweep, right lead closure, Caroli transl;
+ *      with want_transr also the right-to-left sweep and transr)
+ * i.e. the transmission part of negf/phinfortran.f90:1196-1213 and, with
+ * dev_factor = 1, of tb/infortran.f90:490-501 (surface_green + G_block).
+ *
+ * E[npts], qidx[npts] (may be NULL: all q = 0), zero_flag[npts] (may be
+ * NULL) and the outputs transl[npts], transr[npts], status[npts],
+ * iters[2*npts] (left, right iteration counts; may be NULL) are device
+ * arrays.  work must hold pf_transport_tdb_workspace_size(n, nl, nr, npts)
+ * bytes of device memory.  stream is a cudaStream_t (NULL: default stream).
+ * The call is asynchronous on `stream`.
+ */
+size_t pf_transport_tdb_workspace_size(int n, int nl, int nr, int npts);
+
+int pf_transport_tdb_dev(int n, int nl, int nr, int L, int nq,
+                         const double* HL, const double* HLv,
+                         const double* HR, const double* HRv,
+                         const double* Hd, const double* Hdv,
+                         const double* Hld, const double* Hrd,
+                         int npts, const double* E, const int* qidx,
+                         const int* zero_flag,
+                         double eta, double eta0, double dev_factor,
+                         double convergence, int max_iter, int want_transr,
+                         double* transl, double* transr, int* status,
+                         int* iters, void* work, size_t work_bytes,
+                         void* stream);
+
+/*
+ * Same computation with HOST pointers for every array (what the Fortran
+ * driver holds).  Copies in, runs on the current device, copies out and
+ * synchronises.  Device buffers are cached between calls.
+ */
+int pf_transport_tdb(int n, int nl, int nr, int L, int nq,
+                     const double* HL, const double* HLv,
+                     const double* HR, const double* HRv,
+                     const double* Hd, const double* Hdv,
+                     const double* Hld, const double* Hrd,
+                     int npts, const double* E, const int* qidx,
+                     const int* zero_flag,
+                     double eta, double eta0, double dev_factor,
+                     double convergence, int max_iter, int want_transr,
+                     double* transl, double* transr, int* status,
+                     int* iters);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PHINFORTRAN_GB300_H */

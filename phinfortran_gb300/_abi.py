@@ -1,0 +1,73 @@
+"""ctypes binding of the C ABI declared in include/phinfortran_gb300.h.
+
+The shared library is built in-tree by ``phinfortran_gb300.build``.  Loading
+fails loudly when it is missing: there is no CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from .build import LIB
+
+_lib = None
+
+# name -> (restype, argtypes), mirroring include/phinfortran_gb300.h
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+SIGNATURES = {
+    "pf_last_error": (C.c_char_p, []),
+    "pf_version": (C.c_int, []),
+    "pf_transport_tdb_workspace_size": (C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int]),
+    "pf_transport_tdb_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_double, C.c_double, C.c_double, C.c_double,
+                                       C.c_int, C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_size_t, C.c_void_p]),
+    "pf_transport_tdb": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                   _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                   C.c_int, _dp, _ip, _ip,
+                                   C.c_double, C.c_double, C.c_double, C.c_double,
+                                   C.c_int, C.c_int,
+                                   _dp, _dp, _ip, _ip]),
+}
+
+
+class PFError(RuntimeError):
+    """Error reported by the C ABI (message from pf_last_error)."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+def lib_path():
+    return LIB
+
+
+def load():
+    """Load (once) and return the ctypes library handle."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        raise ImportError(
+            f"{LIB} is missing: build it with `python -m phinfortran_gb300.build` "
+            "(the engine has no CPU fallback)")
+    lib = C.CDLL(LIB)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc != 0:
+        msg = load().pf_last_error().decode(errors="replace")
+        raise PFError(rc, msg)
+    return rc

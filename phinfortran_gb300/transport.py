@@ -1,0 +1,163 @@
+"""Host-side mirror of the reference's transport interface over the C ABI.
+
+The reference drives, for every (ie, ik) of its shard,
+
+    call surface_green_tdb_mpi(ie, ik, gl_adv, gr_ret, ..., Egrid, Haml, Hamr, Hamlv, Hamrv)
+    call get_G_full_tdb_mpi(ie, ik, ..., transl_reduce, transr_reduce, ..., hamd, hamdv, hamld, hamrd, haml, hamr)
+
+(negf/phinfortran.f90:1196-1213).  ``transport_tdb`` takes the same blocks
+(as numpy complex128 arrays, one set per q) and the same physics parameters,
+and returns transl/transr for the whole batch of points in one call of the
+fused GPU kernel.  Errors follow the reference's behaviour of stopping on a
+singular or non-finite block (negf/util.f90:29-66): a PFError is raised,
+unless ``check=False`` in which case the per-point status words are returned.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+
+# Block order of the C ABI.
+BLOCK_NAMES = ("HL", "HLv", "HR", "HRv", "Hd", "Hdv", "Hld", "Hrd")
+
+PF_STATUS_SINGULAR = 1
+PF_STATUS_NAN = 2
+PF_STATUS_NOT_CONVERGED = 4
+
+
+def fortran_block(a):
+    """(..., rows, cols) complex -> float64 buffer in column-major block order."""
+    a = np.asarray(a, dtype=np.complex128)
+    return np.ascontiguousarray(np.swapaxes(a, -1, -2)).view(np.float64)
+
+
+@dataclass
+class TdbBlocks:
+    """tdb block set; each array either (m, k) for one q or (nq, m, k)."""
+    HL: np.ndarray
+    HLv: np.ndarray
+    HR: np.ndarray
+    HRv: np.ndarray
+    Hd: np.ndarray    # (L, n, n) or (nq, L, n, n)
+    Hdv: np.ndarray   # (L-1, n, n) or (nq, L-1, n, n)
+    Hld: np.ndarray
+    Hrd: np.ndarray
+
+    @classmethod
+    def from_dict(cls, d):
+        return cls(**{k: d[k] for k in BLOCK_NAMES})
+
+    def stacked(self):
+        """Return (nq, dims, dict of stacked arrays with a leading q axis)."""
+        Hd = np.asarray(self.Hd)
+        if Hd.ndim == 3:
+            arrs = {k: np.asarray(getattr(self, k))[None] for k in BLOCK_NAMES}
+        else:
+            arrs = {k: np.asarray(getattr(self, k)) for k in BLOCK_NAMES}
+        nq, L, n, _ = arrs["Hd"].shape
+        nl = arrs["HL"].shape[-1]
+        nr = arrs["HR"].shape[-1]
+        if arrs["Hdv"].size == 0:
+            arrs["Hdv"] = np.zeros((nq, 0, n, n), np.complex128)
+        _check_shapes(arrs, nq, L, n, nl, nr)
+        return nq, (n, nl, nr, L), arrs
+
+
+def _check_shapes(a, nq, L, n, nl, nr):
+    want = {"HL": (nq, nl, nl), "HLv": (nq, nl, nl), "HR": (nq, nr, nr), "HRv": (nq, nr, nr),
+            "Hd": (nq, L, n, n), "Hdv": (nq, max(L - 1, 0), n, n), "Hld": (nq, nl, n),
+            "Hrd": (nq, nr, n)}
+    for k, shp in want.items():
+        if tuple(a[k].shape) != shp:
+            raise ValueError(f"block {k}: shape {a[k].shape}, expected {shp}")
+
+
+def _ptr(a, ctype=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=None,
+                  zero_flag=None, max_iter=1000, want_transr=True, check=True):
+    """Transmission for a batch of points through the host-pointer C entry.
+
+    E: (npts,) energies (omega^2 for phonons).  blocks: TdbBlocks or dict.
+    qidx: (npts,) q index into the stacked blocks (None: all 0).
+    zero_flag: (npts,) nonzero -> T forced to 0 (the reference's ie == 1).
+    Returns dict(transl, transr, status, iters).
+    """
+    lib = _abi.load()
+    if isinstance(blocks, dict):
+        blocks = TdbBlocks.from_dict(blocks)
+    nq, (n, nl, nr, L), arrs = blocks.stacked()
+    buf = {k: fortran_block(v) for k, v in arrs.items()}
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    npts = E.shape[0]
+    q = None if qidx is None else np.ascontiguousarray(qidx, dtype=np.int32)
+    z = None if zero_flag is None else np.ascontiguousarray(zero_flag, dtype=np.int32)
+    if q is not None and (q.shape != (npts,) or q.min(initial=0) < 0 or q.max(initial=0) >= nq):
+        raise ValueError("qidx out of range")
+    tl = np.zeros(npts)
+    tr = np.zeros(npts)
+    st = np.zeros(npts, dtype=np.int32)
+    it = np.zeros((npts, 2), dtype=np.int32)
+    rc = lib.pf_transport_tdb(n, nl, nr, L, nq, *[_ptr(buf[k]) for k in BLOCK_NAMES], npts, _ptr(E),
+                              None if q is None else _ptr(q, C.c_int),
+                              None if z is None else _ptr(z, C.c_int),
+                              eta, eta0, dev_factor, convergence, max_iter, int(bool(want_transr)),
+                              _ptr(tl), _ptr(tr), _ptr(st, C.c_int), _ptr(it, C.c_int))
+    if rc != 0 and (check or rc != -4):
+        _abi.check(rc)
+    return dict(transl=tl, transr=tr if want_transr else None, status=st, iters=it)
+
+
+class DeviceTransport:
+    """Blocks resident in HBM (torch tensors used only as device buffers).
+
+    ``run`` launches the fused kernel on device-resident energies and writes
+    device-resident outputs: this is the path the throughput benchmark
+    times.  The work queue, scratch and outputs are allocated once.
+    """
+
+    def __init__(self, blocks, npts_max, *, eta, eta0, convergence, dev_factor=10.0,
+                 max_iter=1000, want_transr=False, device="cuda"):
+        import torch
+        self.torch = torch
+        lib = _abi.load()
+        if isinstance(blocks, dict):
+            blocks = TdbBlocks.from_dict(blocks)
+        nq, (n, nl, nr, L), arrs = blocks.stacked()
+        self.dims = (n, nl, nr, L, nq)
+        self.dev = {k: torch.from_numpy(fortran_block(v).copy()).to(device) for k, v in arrs.items()}
+        self.params = (eta, eta0, dev_factor, convergence, max_iter, int(bool(want_transr)))
+        self.npts_max = npts_max
+        ws = lib.pf_transport_tdb_workspace_size(n, nl, nr, npts_max)
+        if ws == 0:
+            _abi.check(-3)
+        self.work = torch.empty(ws, dtype=torch.uint8, device=device)
+        self.transl = torch.zeros(npts_max, dtype=torch.float64, device=device)
+        self.transr = torch.zeros(npts_max, dtype=torch.float64, device=device)
+        self.status = torch.zeros(npts_max, dtype=torch.int32, device=device)
+        self.iters = torch.zeros((npts_max, 2), dtype=torch.int32, device=device)
+
+    def run(self, E, qidx=None, zero_flag=None, stream=None):
+        torch = self.torch
+        lib = _abi.load()
+        n, nl, nr, L, nq = self.dims
+        npts = int(E.shape[0])
+        if npts > self.npts_max:
+            raise ValueError("more points than allocated")
+        s = stream if stream is not None else torch.cuda.current_stream()
+        eta, eta0, dev_factor, conv, max_iter, want_transr = self.params
+        d = self.dev
+        rc = lib.pf_transport_tdb_dev(
+            n, nl, nr, L, nq, *[d[k].data_ptr() for k in BLOCK_NAMES], npts, E.data_ptr(),
+            None if qidx is None else qidx.data_ptr(), None if zero_flag is None else zero_flag.data_ptr(),
+            eta, eta0, dev_factor, conv, max_iter, want_transr,
+            self.transl.data_ptr(), self.transr.data_ptr(), self.status.data_ptr(), self.iters.data_ptr(),
+            self.work.data_ptr(), self.work.numel(), C.c_void_p(s.cuda_stream))
+        _abi.check(rc)
+        return self.transl[:npts], self.transr[:npts], self.status[:npts]

@@ -1,0 +1,56 @@
+"""Generate tests/golden/sisi.npz from the reference's committed si-si example.
+
+Run in a checkout that has the reference at /root/reference:
+
+    python tests/golden/make_golden.py
+
+The fixture holds (a) the processed force constants and supercell of
+examples/negf/si-si (read by the oracle's restatement of negf/fc.f90), and
+(b) the reference's own committed outputs output/trans{l,r}_tot.dat,
+trans{l,r}_{s,ns}.dat and refl{l,r}_{s,ns}.dat (61 omega^2 x 49 k), so the
+GPU tests can check parity on a machine without the reference checkout.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from oracle import qe as Q  # noqa: E402
+
+REF = "/root/reference/examples/negf/si-si"
+
+
+def main(out=os.path.join(HERE, "sisi.npz")):
+    qe = Q.read_qe_fc(os.path.join(REF, "Si444.fc"), r_cutoff=8.3, update_nbr=1)
+    cell_all, pos_all, idxall = Q.build_supercell(qe, 2, 2, 8)
+    mass_id = Q.read_mass_profile(os.path.join(REF, "mass_profile.dat"))
+    mass_no = Q.read_species_masses(os.path.join(REF, "trans_input.fdf"))
+    mass_all = mass_no[mass_id - 1]
+    kg = Q.k_grid_in_ws(Q.k_grid(7, 7), cell_all)
+    E = Q.energy_grid(61, 0.001, 15.5)
+    gold = {}
+    for name in ["transl_tot", "transr_tot", "transl_s", "transl_ns", "transr_s", "transr_ns",
+                 "refll_s", "refll_ns", "reflr_s", "reflr_ns"]:
+        a = np.loadtxt(os.path.join(REF, "output", name + ".dat"))
+        gold[name] = a[:, 1:]
+        gold["E_" + name] = a[:, 0]
+    r_table = np.loadtxt(os.path.join(REF, "fc_qe_r.dat"))
+    np.savez_compressed(
+        out, fc=qe["fc"], cell=qe["cell"], pos=qe["pos"], mass=qe["mass"],
+        nxyz=np.array([qe["nx"], qe["ny"], qe["nz"]]), cell_sc=qe["cell_sc"], rws=qe["rws"], rd=qe["rd"],
+        cell_all=cell_all, pos_all=pos_all, idxall=idxall, mass_all=mass_all, kgrid=kg, E=E,
+        r_table_ref=r_table, r_table_oracle=qe["r_table"],
+        # config of examples/negf/si-si/config
+        eta=1.0e-8, eta0=1.0e-9, convergence=1.17e-14, dev_factor=10.0,
+        n_bloch=np.array([2, 2]), nz=8, buffer=16, period=16, nlayer=2, natm_layer=16,
+        **gold)
+    print("wrote", out)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,45 @@
+"""The C-ABI library builds, loads without a GPU and exports every declared symbol."""
+import ctypes
+import glob
+import os
+import re
+
+from tests.conftest import ROOT
+
+
+def declared_functions():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**\s+\**(pf_[A-Za-z0-9_]+)\s*\(",
+                            src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "pf_transport_tdb" in names and "pf_transport_tdb_dev" in names
+
+
+def test_library_exports_all_declared_symbols(built_lib):
+    lib = ctypes.CDLL(built_lib)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(built_lib):
+    from phinfortran_gb300 import _abi
+    _abi.load()
+    assert set(declared_functions()) <= set(_abi.SIGNATURES)
+
+
+def test_version_and_error_without_gpu(built_lib):
+    from phinfortran_gb300 import _abi
+    lib = _abi.load()
+    assert lib.pf_version() == 1
+    # argument validation runs on the host: no device needed
+    rc = lib.pf_transport_tdb(0, 1, 1, 1, 1, *([None] * 8), 0, None, None, None,
+                              0.0, 0.0, 1.0, 1e-14, 10, 0, None, None, None, None)
+    assert rc == -1
+    assert b"positive" in lib.pf_last_error()

@@ -1,0 +1,145 @@
+"""GPU parity of the fused FP64 transport kernel against the oracle and the
+reference's committed si-si outputs.  Every call goes through the C ABI."""
+import numpy as np
+import pytest
+
+from oracle import negf as N
+from phinfortran_gb300 import systems as S
+from phinfortran_gb300 import transport_tdb
+from phinfortran_gb300._abi import PFError
+from tests.sisi_case import fp64_noise_floor, golden_close, sisi_blocks, sisi_params
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_err(a, b, floor=1e-3):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return np.abs(a - b) / np.maximum(np.abs(b), floor)
+
+
+@pytest.mark.parametrize("ik", [0, 3, 24])
+def test_sisi_against_reference_output(cuda_ready, sisi, ik):
+    b = sisi_blocks(sisi, ik)
+    p = sisi_params(sisi)
+    E = sisi["E"]
+    zf = np.zeros(E.size, np.int32)
+    zf[0] = 1
+    r = transport_tdb(E, b, zero_flag=zf, want_transr=True, **p)
+    assert (r["status"] == 0).all()
+    okl, adl, ql = golden_close(r["transl"], sisi["transl_tot"][:, ik])
+    okr, adr, qr = golden_close(r["transr"], sisi["transr_tot"][:, ik])
+    assert okl, (adl, ql)
+    assert okr, (adr, qr)
+    # and against the oracle on the same inputs (same LAPACK-free algorithm,
+    # different rounding): median 1e-12, every point within the conditioning
+    o = N.transport(E, b, p["eta"], p["eta0"], p["convergence"], p["dev_factor"], zero_first=zf.astype(bool))
+    e = rel_err(r["transl"], o["transl"])
+    assert np.median(e) < 1e-11 and e.max() < 1e-6
+    # iteration counts equal the oracle's (identical stopping rule)
+    assert np.abs(r["iters"][:, 0] - o["iters_left"]).max() <= 1
+
+
+def test_sisi_all_k_multi_q(cuda_ready, sisi):
+    """All 49 k points x 61 omega in one launch (qidx selects the block set)."""
+    ks = list(range(49))
+    bl = [sisi_blocks(sisi, k) for k in ks]
+    stacked = {name: np.stack([x[name] for x in bl]) for name in bl[0]}
+    E1 = sisi["E"]
+    E = np.tile(E1, len(ks))
+    q = np.repeat(np.arange(len(ks)), E1.size).astype(np.int32)
+    zf = np.zeros(E.size, np.int32)
+    zf[::E1.size] = 1
+    r = transport_tdb(E, stacked, qidx=q, zero_flag=zf, want_transr=True, **sisi_params(sisi))
+    TL = r["transl"].reshape(len(ks), E1.size).T
+    TR = r["transr"].reshape(len(ks), E1.size).T
+    okl, adl, ql = golden_close(TL, sisi["transl_tot"])
+    okr, adr, qr = golden_close(TR, sisi["transr_tot"])
+    assert okl, (adl, ql)
+    assert okr, (adr, qr)
+
+
+def test_sc_phonon_workload_parity(cuda_ready):
+    """Simple-cubic bar n=48, L=20 (the FP64 phonon workload) vs the oracle."""
+    b, E, p, _ = S.sc_phonon(ne=256)
+    Es = E[::8]
+    r = transport_tdb(Es, b, want_transr=True, **p)
+    o = N.transport(Es, b, p["eta"], p["eta0"], p["convergence"], p["dev_factor"])
+    assert (r["status"] == 0).all()
+    assert np.median(rel_err(r["transl"], o["transl"])) < 1e-11
+    assert rel_err(r["transl"], o["transl"]).max() < 1e-8
+    assert rel_err(r["transr"], o["transr"]).max() < 1e-8
+
+
+def test_tb_ribbon_workload_parity(cuda_ready):
+    """Electron ribbon n=32, L=200 (the benchmark workload), 64 energies vs the oracle."""
+    b, E, p = S.tb_ribbon()
+    Es = E[::16]
+    r = transport_tdb(Es, b, want_transr=True, **p)
+    o, floor = fp64_noise_floor(Es, b, p)
+    d = np.abs(r["transl"] - o["transl"])
+    assert np.median(rel_err(r["transl"], o["transl"])) < 1e-10
+    # within 20x the FP64 conditioning of each point (absolute 1e-12 minimum)
+    assert (d <= np.maximum(1e-12, 20 * floor)).all(), (d / np.maximum(1e-12, floor)).max()
+
+
+def test_tb_ribbon_full_size_properties(cuda_ready):
+    """All 1024 energies: T_L = T_R (reciprocity), 0 <= T <= channels, pristine => integer."""
+    b, E, p = S.tb_ribbon()
+    r = transport_tdb(E, b, want_transr=True, **p)
+    assert (r["status"] == 0).all()
+    d = np.abs(r["transl"] - r["transr"])
+    assert np.median(d) < 1e-10 and d.max() < 1e-4
+    assert r["transl"].min() >= 0 and r["transl"].max() <= 32 + 1e-6
+    b0, E0, p0 = S.tb_ribbon(disorder=0.0, L=50, ne=1000)
+    r0 = transport_tdb(E0, b0, want_transr=False, **p0)
+    # integer channel counts away from the subband edges 2cos(m pi/33) +- 2
+    eps = 2 * np.cos(np.arange(1, 33) * np.pi / 33)
+    edges = np.concatenate([eps - 2, eps + 2])
+    away = np.array([np.abs(edges - e).min() > 1e-2 for e in E0])
+    assert np.abs(r0["transl"][away] - np.round(r0["transl"][away])).max() < 1e-6
+
+
+def test_edge_cases(cuda_ready):
+    # single device layer (no Hdv), uneven lead and device widths
+    rng = np.random.default_rng(5)
+    n, nl, nr = 6, 4, 5
+
+    def herm(m):
+        a = rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m))
+        return a + a.conj().T
+
+    blocks = dict(HL=herm(nl), HLv=rng.normal(size=(nl, nl)) * 0.5, HR=herm(nr),
+                  HRv=rng.normal(size=(nr, nr)) * 0.5, Hd=herm(n)[None], Hdv=np.zeros((0, n, n)),
+                  Hld=rng.normal(size=(nl, n)) * 0.5, Hrd=rng.normal(size=(nr, n)) * 0.5)
+    E = np.linspace(-3, 3, 13)
+    r = transport_tdb(E, blocks, eta=0.0, eta0=1e-3, convergence=1e-12, dev_factor=1.0, want_transr=True)
+    o = N.transport(E, blocks, 0.0, 1e-3, 1e-12, 1.0)
+    assert np.abs(r["transl"] - o["transl"]).max() < 1e-10
+    assert np.abs(r["transr"] - o["transr"]).max() < 1e-10
+    # empty batch is a no-op
+    r = transport_tdb(np.zeros(0), blocks, eta=0.0, eta0=1e-3, convergence=1e-12, dev_factor=1.0)
+    assert r["transl"].size == 0
+
+
+def test_status_flags(cuda_ready):
+    b, E, p = S.tb_ribbon(W=8, L=4, ne=8)
+    # iteration cap -> not-converged flag, reported per point, call raises
+    with pytest.raises(PFError):
+        transport_tdb(E, b, max_iter=2, **p)
+    r = transport_tdb(E, b, max_iter=2, check=False, **p)
+    assert (r["status"] & 4).any()
+    # a NaN in the device block -> NaN flag on every point
+    bn = dict(b)
+    bn["Hd"] = b["Hd"].copy()
+    bn["Hd"][1, 0, 0] = np.nan
+    r = transport_tdb(E, bn, check=False, **p)
+    assert (r["status"] & 2).all()
+    # an exactly singular device block -> singular flag
+    bs = {k: v.copy() for k, v in b.items()}
+    bs["Hd"][:] = 0.0
+    bs["Hdv"][:] = 0.0
+    bs["Hld"][:] = 0.0
+    bs["Hrd"][:] = 0.0
+    r = transport_tdb(np.zeros(2), bs, eta=0.0, eta0=0.0, convergence=1e-14, dev_factor=1.0, check=False)
+    assert (r["status"] & 1).all()
