@@ -1,0 +1,366 @@
+"""Throughput benchmark of the NEGF transport hot path on GB300.
+
+Workload: the electron ribbon of the headline metric -- single-orbital
+nearest-neighbour square lattice, width 32 (n = 32 per slice), 200 device
+slices with Anderson disorder U[-0.5, 0.5]|t|, t = -1, 1024 energies on
+[-4.2, 4.2]|t|, eta = 1e-6 (synthetic, seeded).  One step = one pass of the
+hot path over the whole 1024-point batch: both lead decimations, the
+left-to-right RGF sweep and the Caroli trace for every energy, i.e. one
+T(E) per (E, q) point ("solve").
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--path mixed|fp64]
+    python bench.py --impl reference ...   (CPU oracle on the host cores)
+
+Rank 0 prints one JSON line.  `value` = solves/s of the headline path
+(default: mixed precision -- double-float leads, FP32 factorisation, one
+double-float refinement sweep) with inputs resident in HBM (CUDA events
+around each step on the launching stream, L2 flushed before every step);
+`e2e` = the same through the host-pointer C entry with host buffers, copies
+inside the timed region; `compare` = the plain FP64 path on the same batch
+(speed-up and the accuracy of the headline T(E) against it).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(workload="tb_ribbon_W32_L200_1024E", n=32, L=200, ne=1024, W=32, t=-1.0,
+                disorder=0.5, emin=-4.2, emax=4.2, eta=1e-6, convergence=1e-14)
+METRIC = "RGF (omega,q) solves/s (T(E) per point), tb ribbon n=32 L=200, 1024 E"
+
+
+def flops_per_solve(n, L, I):
+    """Algorithmic real flops of one solve: n^3 (40 L + 16) + 2 n^3 (56 I + 24)."""
+    return n ** 3 * (40 * L + 16) + 2 * n ** 3 * (56 * I + 24)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return dict(sm_mhz=None, sm_max_mhz=None, reasons=["nvidia-smi unavailable"], samples=0)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return dict(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=smax,
+                    reasons=sorted(reasons), samples=len(sm))
+
+
+def measure_peak(torch, dtype, n):
+    """Live cuBLAS GEMM rate (TFLOP/s) used as the roofline denominator."""
+    a = torch.randn(n, n, dtype=dtype, device="cuda")
+    b = torch.randn(n, n, dtype=dtype, device="cuda")
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        a @ b
+        e.record()
+        torch.cuda.synchronize()
+        best = min(best, s.elapsed_time(e) * 1e-3)
+    mult = 8 if dtype.is_complex else 2
+    return mult * n ** 3 / best / 1e12
+
+
+def cpu_oracle_rate(E, blocks, p, budget_s=12.0, min_pts=16):
+    """Oracle solves/s on the host cores for a bounded sample of the workload."""
+    from oracle import negf as N
+    try:
+        from threadpoolctl import threadpool_info
+        cores = max([i.get("num_threads", 1) for i in threadpool_info()] or [1])
+    except Exception:  # noqa: BLE001
+        cores = os.cpu_count() or 1
+    npts = min_pts
+    idx = np.linspace(0, len(E) - 1, npts).astype(int)
+    t0 = time.perf_counter()
+    N.transport(E[idx], blocks, p["eta"], p["eta0"], p["convergence"], p["dev_factor"], want_plus_minus=False)
+    dt = time.perf_counter() - t0
+    # grow the sample to roughly `budget_s` of CPU work
+    if dt < budget_s / 2:
+        npts2 = int(min(len(E), max(npts, npts * budget_s / max(dt, 1e-3))))
+        idx = np.linspace(0, len(E) - 1, npts2).astype(int)
+        t0 = time.perf_counter()
+        N.transport(E[idx], blocks, p["eta"], p["eta0"], p["convergence"], p["dev_factor"],
+                    want_plus_minus=False)
+        dt = time.perf_counter() - t0
+        npts = npts2
+    return npts / dt, cores, f"{npts} of {len(E)} energies (uniform stride), T_L only, numpy FP64 oracle"
+
+
+def build_workload():
+    from phinfortran_gb300 import systems
+    w = WORKLOAD
+    b, E, p = systems.tb_ribbon(W=w["W"], L=w["L"], t=w["t"], disorder=w["disorder"], ne=w["ne"],
+                                emin=w["emin"], emax=w["emax"], eta=w["eta"], convergence=w["convergence"])
+    return b, E, p
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    b, E, p = build_workload()
+    vals = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        v, cores, sample = cpu_oracle_rate(E, b, p, budget_s=args.ref_budget)
+        info = (cores, sample)
+        if i >= args.warmup:
+            vals.append(v)
+    v = statistics.median(vals)
+    line = dict(metric=METRIC, value=v, unit="solves/s", n_gpus=args.gpus, steps=args.steps,
+                warmup=args.warmup, ms_per_step=1e3 * WORKLOAD["ne"] / v, higher_is_better=True,
+                scaling="weak", vs_baseline=None, dtype="complex128", data="synthetic (seeded)",
+                config=dict(workload=WORKLOAD["workload"], n=32, L=200, energies=1024, eta=1e-6),
+                impl="reference",
+                cpu_baseline=dict(value=v, unit="solves/s", cores=info[0], kind="port", sample=info[1]),
+                e2e=dict(value=v, unit="solves/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0),
+                note="reference Fortran/MPI/MKL build is not compilable here (no Fortran, MPI or LAPACK); "
+                     "the timed CPU implementation is the FP64 numpy restatement of the path")
+    print(json.dumps(line), flush=True)
+
+
+def time_steps(torch, fn, steps, flush, stream):
+    times = []
+    for _ in range(steps):
+        flush.zero_()                       # evict L2 (256 MB > 129 MB) outside the timed window
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        fn()
+        e.record(stream)
+        torch.cuda.synchronize()
+        times.append(s.elapsed_time(e) * 1e-3)
+    return times
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--path", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--refine", type=int, default=1, help="refinement sweeps of the mixed path")
+    ap.add_argument("--ref-budget", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the FP64 comparison path (accuracy and speed-up fields)")
+    ap.add_argument("--energies", type=int, default=0,
+                    help="use only N energies of the workload (profiling runs)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from phinfortran_gb300 import DeviceTransport, transport_tdb
+    from phinfortran_gb300.transport import TdbBlocks, fortran_block
+
+    b, E, p = build_workload()
+    if args.energies:
+        E = E[np.linspace(0, len(E) - 1, args.energies).astype(int)]
+    npts = len(E)
+    Ed = torch.from_numpy(E).to("cuda")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(t):
+        if ws > 1:
+            tt = torch.tensor([t], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            return tt.item()
+        return t
+
+    main_dt = DeviceTransport(b, npts, want_transr=False, precision=args.path, refine_iters=args.refine, **p)
+    for _ in range(args.warmup):
+        main_dt.run(Ed, stream=stream)
+    torch.cuda.synchronize()
+    iters = main_dt.iters[:npts].float().mean().item()
+    status = main_dt.status[:npts].cpu().numpy()
+    T_main = main_dt.transl[:npts].cpu().numpy().copy()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    times = time_steps(torch, lambda: main_dt.run(Ed, stream=stream), args.steps, flush, stream)
+    barrier()
+    clk = clocks.stop()
+    t_step = max_over_ranks(sum(times) / len(times))
+    value = ws * npts / t_step
+
+    # ---- FP64 comparison path: speed-up and accuracy of the headline path ----
+    compare = None
+    if not args.no_compare:
+        f64 = DeviceTransport(b, npts, want_transr=False, precision="fp64", **p) if args.path != "fp64" else main_dt
+        for _ in range(1 if f64 is not main_dt else 0):
+            f64.run(Ed, stream=stream)
+        torch.cuda.synchronize()
+        t64 = time_steps(torch, lambda: f64.run(Ed, stream=stream), max(1, min(args.steps, 3)), flush, stream)
+        T64 = f64.transl[:npts].cpu().numpy().copy()
+        # FP64 conditioning of every point: rerun with every block perturbed by ~1e-15 relative
+        rng = np.random.default_rng(123)
+        bp = {k: np.asarray(v) * (1 + 1e-15 * rng.standard_normal(np.shape(v))) for k, v in b.items()}
+        fp = DeviceTransport(bp, npts, want_transr=False, precision="fp64", **p)
+        fp.run(Ed, stream=stream)
+        torch.cuda.synchronize()
+        floor = np.abs(fp.transl[:npts].cpu().numpy() - T64)
+        rel = np.abs(T_main - T64) / np.maximum(np.abs(T64), 1e-3)
+        good = floor / np.maximum(np.abs(T64), 1e-3) <= 1e-10
+        compare = dict(
+            fp64_solves_per_s=ws * npts / max_over_ranks(sum(t64) / len(t64)),
+            fp64_ms_per_step=1e3 * sum(t64) / len(t64),
+            speedup_vs_fp64=(ws * npts / t_step) / (ws * npts / max_over_ranks(sum(t64) / len(t64))),
+            accuracy=dict(reference="FP64 GPU path, same energies", metric="|T-T64|/max(|T64|,1e-3)",
+                          median=float(np.median(rel)), q99=float(np.quantile(rel, 0.99)), max=float(rel.max()),
+                          frac_le_1e_8=float((rel <= 1e-8).mean()),
+                          fp64_conditioned_points=int(good.sum()),
+                          frac_le_1e_8_where_fp64_reproducible=float((rel[good] <= 1e-8).mean()) if good.any() else None,
+                          max_where_fp64_reproducible=float(rel[good].max()) if good.any() else None,
+                          note="points are 'fp64 reproducible' when a 1e-15 relative perturbation of the inputs "
+                               "moves the FP64 result by <= 1e-10 relative"))
+
+    # ---- end to end through the host-pointer C entry ----
+    nq, dims, arrs = TdbBlocks.from_dict(b).stacked()
+    h2d = sum(fortran_block(v).nbytes for v in arrs.values()) + E.nbytes
+    d2h = npts * 8 + npts * 4 + npts * 8      # transl, status, iterations
+    call = lambda: transport_tdb(E, b, want_transr=False, precision=args.path, refine_iters=args.refine, **p)
+    for _ in range(0 if args.no_e2e else 2):
+        call()
+    barrier()
+    e2e_t = [float("inf")] if args.no_e2e else []
+    for _ in range(0 if args.no_e2e else args.steps):
+        t0 = time.perf_counter()
+        call()
+        e2e_t.append(time.perf_counter() - t0)
+    barrier()
+    t_e2e = max_over_ranks(sum(e2e_t) / len(e2e_t))
+    e2e_value = ws * npts / t_e2e
+
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    n, L = WORKLOAD["n"], WORKLOAD["L"]
+    fl = flops_per_solve(n, L, iters) * npts
+    achieved = fl / t_step / 1e12
+    if args.path == "fp64":
+        peak = measure_peak(torch, torch.complex128, 2048)
+        peak_src = ("cuBLAS ZGEMM 2048^3 measured live on this GPU (FP64 pipe; MEASURED_PEAKS.json holds only "
+                    "bf16 and HBM figures)")
+        kernel = "transport_kernel<double>"
+    else:
+        torch.backends.cuda.matmul.allow_tf32 = False
+        peak = measure_peak(torch, torch.complex64, 4096)
+        peak_src = ("cuBLAS CGEMM 4096^3 (FP32 SIMT, TF32 off) measured live on this GPU: the mixed kernel runs "
+                    "on the FP32 pipe (FP32 and double-float arithmetic); achieved counts the FP64-equivalent "
+                    "algorithmic flops F(n,L,I) only")
+        kernel = "mixed_kernel"
+    roof = dict(bound="tensor", achieved=achieved, peak=peak, unit="TFLOP/s", frac=achieved / peak, traffic=None,
+                peak_source=peak_src, kernel=kernel, algorithmic_flops_per_launch=fl,
+                flops_formula="n^3 (40 L + 16) + 2 n^3 (56 I + 24)", mean_decimation_iters=iters)
+    prof = os.path.join(ROOT, "profiles", f"{args.path}_kernel_tb_ribbon.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            pj = json.load(f)
+        roof["traffic"] = pj.get("dram_bytes_per_launch_scaled")
+        roof["traffic_source"] = pj.get("source")
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, cores, sample = cpu_oracle_rate(E, b, p)
+        cpu = dict(value=v, unit="solves/s", cores=cores, kind="port", sample=sample)
+
+    launches_per_step = 1 if args.path == "fp64" else 9   # mixed: 8 block conversions + 1 transport kernel
+    line = dict(metric=METRIC, value=value, unit="solves/s", n_gpus=ws, steps=args.steps, warmup=args.warmup,
+                ms_per_step=t_step * 1e3, higher_is_better=True, scaling="weak", vs_baseline=None,
+                dtype="complex128 (fp64)" if args.path == "fp64" else "complex: fp32 + double-float (no fp64 ops)",
+                data="synthetic (seeded PCG64)",
+                config=dict(workload=WORKLOAD["workload"], n=n, L=L, energies=npts, eta=1e-6, path=args.path,
+                            refine_iters=args.refine if args.path == "mixed" else None,
+                            l2="flushed (256 MB write) before every timed step", parallelism=f"replicas x{ws}"),
+                e2e=dict(value=e2e_value, unit="solves/s", h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
+                         entry="pf_transport_tdb_mixed" if args.path == "mixed" else "pf_transport_tdb"),
+                roofline=roof, cpu_baseline=cpu, compare=compare,
+                clocks=dict(sm_mhz=clk["sm_mhz"], sm_max_mhz=clk["sm_max_mhz"], reasons=clk["reasons"]),
+                gpu_launches=launches_per_step * args.steps, status_nonzero=int((status != 0).sum()))
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -114,6 +114,47 @@ int pf_transport_tdb(int n, int nl, int nr, int L, int nq,
                      double* transl, double* transr, int* status,
                      int* iters);
 
+/*
+ * Mixed-precision transport (T_L only), device pointers.  Same inputs and
+ * meaning as pf_transport_tdb_dev; the arithmetic differs:
+ *   - both lead decimations run in double-float (pairs of FP32 numbers,
+ *     ~48-bit significand) -- the FP64 algorithm of negf/surface.f90:488-497;
+ *   - the device blocks are factorised in FP32 (the left-connected
+ *     recursion of negf/lesser.f90:547-654 as a block LU of the extended
+ *     lead+device matrix), and the last block column G_{:,N+1} is refined
+ *     `refine_iters` times against a double-float residual;
+ *   - the Caroli trace (negf/lesser.f90:787-792) is taken in double-float.
+ * The per-point matrix work uses no FP64 arithmetic.  work must hold
+ * pf_transport_tdb_mixed_workspace_size(...) bytes.
+ */
+size_t pf_transport_tdb_mixed_workspace_size(int n, int nl, int nr, int L,
+                                             int nq, int npts);
+
+int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq,
+                               const double* HL, const double* HLv,
+                               const double* HR, const double* HRv,
+                               const double* Hd, const double* Hdv,
+                               const double* Hld, const double* Hrd,
+                               int npts, const double* E, const int* qidx,
+                               const int* zero_flag,
+                               double eta, double eta0, double dev_factor,
+                               double convergence, int max_iter,
+                               int refine_iters, double* transl, int* status,
+                               int* iters, void* work, size_t work_bytes,
+                               void* stream);
+
+/* Host-pointer variant of pf_transport_tdb_mixed_dev (synchronous). */
+int pf_transport_tdb_mixed(int n, int nl, int nr, int L, int nq,
+                           const double* HL, const double* HLv,
+                           const double* HR, const double* HRv,
+                           const double* Hd, const double* Hdv,
+                           const double* Hld, const double* Hrd,
+                           int npts, const double* E, const int* qidx,
+                           const int* zero_flag,
+                           double eta, double eta0, double dev_factor,
+                           double convergence, int max_iter, int refine_iters,
+                           double* transl, int* status, int* iters);
+
 #ifdef __cplusplus
 }
 #endif

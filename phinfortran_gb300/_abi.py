@@ -27,6 +27,21 @@ SIGNATURES = {
                                        C.c_int, C.c_int,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_size_t, C.c_void_p]),
+    "pf_transport_tdb_mixed_workspace_size": (C.c_size_t, [C.c_int] * 6),
+    "pf_transport_tdb_mixed_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_double, C.c_double, C.c_double, C.c_double,
+                                             C.c_int, C.c_int,
+                                             C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_size_t, C.c_void_p]),
+    "pf_transport_tdb_mixed": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                         _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                         C.c_int, _dp, _ip, _ip,
+                                         C.c_double, C.c_double, C.c_double, C.c_double,
+                                         C.c_int, C.c_int,
+                                         _dp, _ip, _ip]),
     "pf_transport_tdb": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                    _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                    C.c_int, _dp, _ip, _ip,

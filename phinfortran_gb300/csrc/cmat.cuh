@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "df64.cuh"
+
 namespace pf {
 
 template <typename R>
@@ -58,9 +60,10 @@ template <typename R>
 __device__ __forceinline__ cx<R> cfma(cx<R> a, cx<R> b, cx<R> c) {
   return mk<R>(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
 }
+// |re| + |im| in double (pivot choice, like LAPACK's izamax)
 template <typename R>
-__device__ __forceinline__ R cabs1(cx<R> a) {
-  return fabs(a.x) + fabs(a.y);
+__device__ __forceinline__ double cabs1(cx<R> a) {
+  return fabs(to_d(a.x)) + fabs(to_d(a.y));
 }
 // 1/a by Smith's scaled division (no overflow for large |a|).
 template <typename R>
@@ -77,7 +80,7 @@ __device__ __forceinline__ cx<R> crecip(cx<R> a) {
 }
 template <typename R>
 __device__ __forceinline__ cx<R> shfl(cx<R> v, int src) {
-  return mk<R>(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+  return mk<R>(shfl_r(v.x, src), shfl_r(v.y, src));
 }
 
 // Generic operand: pointer + leading dimension + conjugate-transpose flag.
@@ -232,19 +235,25 @@ __device__ void shift_neg(cx<R>* dst, int ldd, cx<R> z, const cx<R>* src, int ld
   __syncthreads();
 }
 
-// max_ij |a_ij| (modulus), block reduction through `red` (>= 32 entries).
+// |a| for convergence tests: FP64 for double data, FP32 otherwise (a df64
+// value's leading float carries its magnitude to ~1e-7).
+__device__ __forceinline__ double abs_for_max(cx<double> e) { return hypot(e.x, e.y); }
+__device__ __forceinline__ double abs_for_max(cx<float> e) { return (double)hypotf(e.x, e.y); }
+__device__ __forceinline__ double abs_for_max(cx<df64> e) { return (double)hypotf(e.x.hi, e.y.hi); }
+
+// max_ij |a_ij| (modulus), block reduction through
+// `red` (>= 32 doubles).  A NaN entry makes the result NaN.
 template <typename R>
-__device__ R max_abs(const cx<R>* a, int ld, int m, int n, R* red) {
-  R v = R(0);
+__device__ double max_abs(const cx<R>* a, int ld, int m, int n, double* red) {
+  double v = 0.0;
   for (int i = threadIdx.x; i < m * n; i += blockDim.x) {
     const int r = i % m, c = i / m;
     const cx<R> e = a[r + c * ld];
-    const R h = hypot(e.x, e.y);
-    // a NaN entry propagates as NaN so callers can flag it
+    const double h = abs_for_max(e);
     v = (h > v || h != h) ? h : v;
   }
   for (int o = 16; o > 0; o >>= 1) {
-    const R w = __shfl_xor_sync(0xffffffffu, v, o);
+    const double w = __shfl_xor_sync(0xffffffffu, v, o);
     v = (w > v || w != w) ? w : v;
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -252,9 +261,9 @@ __device__ R max_abs(const cx<R>* a, int ld, int m, int n, R* red) {
   if (lane == 0) red[warp] = v;
   __syncthreads();
   if (warp == 0) {
-    v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : R(0);
+    v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.0;
     for (int o = 16; o > 0; o >>= 1) {
-      const R w = __shfl_xor_sync(0xffffffffu, v, o);
+      const double w = __shfl_xor_sync(0xffffffffu, v, o);
       v = (w > v || w != w) ? w : v;
     }
     if (lane == 0) red[0] = v;
@@ -292,18 +301,18 @@ __device__ int inverse(cx<R>* M, int ld, int n, InvWork<R> w) {
   for (int k = 0; k < n; ++k) {
     // (a) pivot search on column k, rows k..n-1 (first maximum, |re|+|im|)
     if (warp == 0) {
-      R best = R(-1);
+      double best = -1.0;
       int bi = k;
       for (int i = k + lane; i < n; i += 32) {
-        const R v = cabs1(M[i + k * ld]);
-        const R vv = (v != v) ? R(3.0e300) : v;  // NaN wins so it gets reported
+        const double v = cabs1(M[i + k * ld]);
+        const double vv = (v != v) ? 3.0e300 : v;  // NaN wins so it gets reported
         if (vv > best) {
           best = vv;
           bi = i;
         }
       }
       for (int o = 16; o > 0; o >>= 1) {
-        const R ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
         const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
         if (ob > best || (ob == best && oi < bi)) {
           best = ob;
@@ -369,15 +378,16 @@ __device__ int inverse(cx<R>* M, int ld, int n, InvWork<R> w) {
   return status;
 }
 
-// Re Tr(X * Y) with X (m x n) and Y (n x m), block reduction via `red`.
+// Re Tr(X * Y) with X (m x n) and Y (n x m), accumulated in double,
+// block reduction via `red` (>= 32 doubles).
 template <typename R>
-__device__ R trace_prod_re(const cx<R>* X, int ldx, Op<R> Y, int m, int n, R* red) {
-  R v = R(0);
+__device__ double trace_prod_re(const cx<R>* X, int ldx, Op<R> Y, int m, int n, double* red) {
+  double v = 0.0;
   for (int i = threadIdx.x; i < m * n; i += blockDim.x) {
     const int r = i % m, c = i / m;
     const cx<R> a = X[r + c * ldx];
     const cx<R> b = Y.at(c, r);
-    v += a.x * b.x - a.y * b.y;
+    v += to_d(a.x) * to_d(b.x) - to_d(a.y) * to_d(b.y);
   }
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -385,7 +395,7 @@ __device__ R trace_prod_re(const cx<R>* X, int ldx, Op<R> Y, int m, int n, R* re
   if (lane == 0) red[warp] = v;
   __syncthreads();
   if (warp == 0) {
-    v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : R(0);
+    v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.0;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) red[0] = v;
   }

@@ -1,0 +1,336 @@
+// Mixed-precision point pipeline (FP32 + double-float, no FP64 instructions
+// on the hot path).
+//
+// The transmission T_L = Re Tr[G_{0,N+1} Gamma_R G_{0,N+1}^H Gamma_L] of
+// negf/lesser.f90:787-792 only needs the last block column
+// X = A^{-1} E_{N+1} of the extended block-tridiagonal matrix A over the
+// layers j = 0 (left lead cell), 1..L (device), L+1 (right lead cell):
+//   A_00      = gl^{-1} = conj(z_adv) - es_adv^H   (es: decimated onsite)
+//   A_jj      = z_D - Hd_j                        (j = 1..L)
+//   A_{L+1}   = z_D - HR - Sigma_R                (lesser.f90:617)
+//   A_{j,j+1} = -V_j  with V_0 = Hld, V_j = Hdv_j, V_L = Hrd^H.
+// The reference's left-connected recursion (lesser.f90:547-654) is the
+// forward block-LU of this matrix, so G_{0,N+1} = X_0.
+//
+// Stages per point:
+//   1. both lead decimations in df64 (the FP64 algorithm of
+//      negf/surface.f90:488-497; FP32 cannot resolve eta ~ 1e-6);
+//   2. FP32 block LU: g_j = inv(A_jj - V_{j-1}^H g_{j-1} V_{j-1}), stored;
+//   3. FP32 back substitution X_{L+1} = g_{L+1}, X_j = g_j V_j X_{j+1};
+//   4. `nref` refinement sweeps: residual r = E_{N+1} - A X in df64,
+//      correction by the stored FP32 factors, X += dX in df64;
+//   5. Caroli trace in df64.
+#pragma once
+#include "transport.cuh"
+
+namespace pf {
+
+using dcx = cx<df64>;
+using fcx = cx<float>;
+
+// Block set converted once per call: df64 copies (residual, leads, Caroli)
+// and FP32 copies (factorisation and corrections), same layout as the
+// FP64 input (column-major, ld = rows).
+struct MSys {
+  int n, nl, nr, L, nq;
+  const dcx *HL, *HLv, *HR, *HRv, *Hd, *Hdv, *Hld, *Hrd;
+  const fcx *fHR, *fHd, *fHdv, *fHld, *fHrd;
+};
+
+enum { NSM_M = 6 };
+// per-CTA df64 scratch matrices
+enum { M_E1 = 0, M_ES, M_W2, M_W3, M_ESL, M_GML, M_GMR, M_SR, M_R, NGM };
+
+struct MCtx {
+  dcx* sm[NSM_M];      // shared slots, sized for df64 (reused as FP32)
+  dcx* gs[NGM];        // per-CTA df64 scratch
+  fcx* lu;             // (L+2) FP32 factors g_j
+  fcx* yv;             // (L+2) FP32 forward vectors
+  dcx* xv;             // (L+2) df64 solution blocks X_j
+  fcx* fsr;            // FP32 copy of Sigma_R
+  int ld;
+  size_t mat;          // elements per matrix slot
+  InvWork<df64> iwd;
+  InvWork<float> iwf;
+  double* red;
+};
+
+__device__ __forceinline__ fcx f_of(dcx a) { return mk<float>(a.x.hi, a.y.hi); }
+__device__ __forceinline__ dcx d_of(fcx a) { return mk<df64>(df64(a.x, 0.f), df64(a.y, 0.f)); }
+
+// dst(float) = src(df64) or its conjugate transpose
+__device__ void cvt_df_to_f(fcx* dst, int ldd, bool conj_t, const dcx* src, int lds, int m, int n) {
+  for (int i = threadIdx.x; i < m * n; i += blockDim.x) {
+    const int r = i % m, c = i / m;
+    const dcx v = conj_t ? cconj(src[c + r * lds]) : src[r + c * lds];
+    dst[r + (size_t)c * ldd] = f_of(v);
+  }
+  __syncthreads();
+}
+__device__ void cvt_f_to_df(dcx* dst, int ldd, const fcx* src, int lds, int m, int n) {
+  for (int i = threadIdx.x; i < m * n; i += blockDim.x) {
+    const int r = i % m, c = i / m;
+    dst[r + (size_t)c * ldd] = d_of(src[r + c * lds]);
+  }
+  __syncthreads();
+}
+
+// Epilogue: C(float) = acc + add(r,c)   (add from a float matrix, optional)
+struct EpiStoreAddF {
+  fcx* c;
+  int ld;
+  const fcx* add;
+  int ldadd;
+  __device__ __forceinline__ void operator()(int r, int col, fcx acc) const {
+    fcx v = acc;
+    if (add) v = cadd(v, add[r + col * ldadd]);
+    c[r + col * ld] = v;
+  }
+};
+// Epilogue of the backward correction: d = acc + y (float); stores d and
+// accumulates X += d in df64.
+struct EpiCorr {
+  fcx* d;
+  int ld;
+  const fcx* y;
+  dcx* x;
+  __device__ __forceinline__ void operator()(int r, int col, fcx acc) const {
+    const fcx v = cadd(acc, y[r + col * ld]);
+    d[r + col * ld] = v;
+    dcx xv = x[r + col * ld];
+    xv.x = xv.x + df64(v.x, 0.f);
+    xv.y = xv.y + df64(v.y, 0.f);
+    x[r + col * ld] = xv;
+  }
+};
+// Residual start: R = acc + b - z X   (b = I on the last layer)
+struct EpiRes0 {
+  dcx* r;
+  int ld;
+  const dcx* X;
+  dcx z;
+  bool ident;
+  __device__ __forceinline__ void operator()(int i, int col, dcx acc) const {
+    const dcx xv = X[i + col * ld];
+    dcx v = csub(acc, cmul(z, xv));
+    if (ident && i == col) v.x = v.x + df64(1.f, 0.f);
+    r[i + col * ld] = v;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Lead decimations in df64.  Results left in per-CTA scratch:
+//   M_ESL = es_adv^H (df64), M_GML = -gml_adv, M_GMR = gmr_ret, M_SR = sr_ret,
+//   lu[0] = gl_ret = g_adv^H (FP32), fsr = FP32 sr_ret.
+// ---------------------------------------------------------------------------
+template <int S>
+__device__ int mixed_leads(const MCtx& mc, const MSys& sys, int q, double E, const Params& P, int* it_l,
+                           int* it_r) {
+  Ctx<df64> c;
+  for (int i = 0; i < NSM; ++i) c.sm[i] = mc.sm[i];
+  c.gs[G_E1] = mc.gs[M_E1];
+  c.gs[G_ES] = mc.gs[M_ES];
+  c.gs[G_W2] = mc.gs[M_W2];
+  c.gs[G_W3] = mc.gs[M_W3];
+  c.ld = mc.ld;
+  c.iw = mc.iwd;
+  c.red = mc.red;
+  const int ld = mc.ld, nl = sys.nl, nr = sys.nr;
+  const double eps = E * P.eta + P.eta0;
+  int st = PF_OK;
+  {
+    const dcx* HL = sys.HL + (size_t)q * nl * nl;
+    const dcx* HLv = sys.HLv + (size_t)q * nl * nl;
+    st |= decimate<df64, S>(c, nl, mk<df64>(df64(E), df64(-eps)), opN<df64>(HL, nl), opC<df64>(HLv, nl),
+                            opN<df64>(HLv, nl), P.convergence, P.max_iter, it_l);
+    cvt_df_to_f(mc.lu, ld, true, c.sm[2], ld, nl, nl);          // g_0 = g_adv^H
+    copy_out(mc.gs[M_ESL], ld, true, c.gs[G_ES], ld, nl, nl);   // es_adv^H
+    lead_sigma<df64, S>(c, nl, HLv);                            // SM1 = sl_adv
+    gamma_from_sigma(mc.gs[M_GML], ld, c.sm[1], ld, nl, -1);
+  }
+  {
+    const dcx* HR = sys.HR + (size_t)q * nr * nr;
+    const dcx* HRv = sys.HRv + (size_t)q * nr * nr;
+    st |= decimate<df64, S>(c, nr, mk<df64>(df64(E), df64(eps)), opN<df64>(HR, nr), opC<df64>(HRv, nr),
+                            opN<df64>(HRv, nr), P.convergence, P.max_iter, it_r);
+    lead_sigma<df64, S>(c, nr, HRv);                            // SM1 = sr_ret
+    copy_out(mc.gs[M_SR], ld, false, c.sm[1], ld, nr, nr);
+    cvt_df_to_f(mc.fsr, ld, false, c.sm[1], ld, nr, nr);
+    gamma_from_sigma(mc.gs[M_GMR], ld, c.sm[1], ld, nr, +1);
+  }
+  return st;
+}
+
+// Dimension of extended layer j.
+__device__ __forceinline__ int ext_dim(const MSys& s, int j) { return j == 0 ? s.nl : (j == s.L + 1 ? s.nr : s.n); }
+
+// Coupling V_j = -A_{j,j+1} (rows dim(j), cols dim(j+1)) as an FP32 operand.
+__device__ __forceinline__ Op<float> vf(const MSys& s, int q, int j) {
+  const int n = s.n, L = s.L;
+  if (j == 0) return opN<float>(s.fHld + (size_t)q * s.nl * n, s.nl);
+  if (j == L) return opC<float>(s.fHrd + (size_t)q * s.nr * n, s.nr);
+  return opN<float>(s.fHdv + ((size_t)q * (L - 1) + (j - 1)) * n * n, n);
+}
+__device__ __forceinline__ Op<float> vf_h(const MSys& s, int q, int j) {
+  Op<float> o = vf(s, q, j);
+  o.ct = !o.ct;
+  return o;
+}
+__device__ __forceinline__ Op<df64> vd(const MSys& s, int q, int j) {
+  const int n = s.n, L = s.L;
+  if (j == 0) return opN<df64>(s.Hld + (size_t)q * s.nl * n, s.nl);
+  if (j == L) return opC<df64>(s.Hrd + (size_t)q * s.nr * n, s.nr);
+  return opN<df64>(s.Hdv + ((size_t)q * (L - 1) + (j - 1)) * n * n, n);
+}
+__device__ __forceinline__ Op<df64> vd_h(const MSys& s, int q, int j) {
+  Op<df64> o = vd(s, q, j);
+  o.ct = !o.ct;
+  return o;
+}
+
+// ---------------------------------------------------------------------------
+// Stage 2+3: FP32 block LU of the extended system and back substitution.
+// ---------------------------------------------------------------------------
+template <int S>
+__device__ int mixed_factor_solve(const MCtx& mc, const MSys& sys, int q, fcx zD) {
+  const int ld = mc.ld, L = sys.L;
+  const size_t mat = mc.mat;
+  fcx* sV = reinterpret_cast<fcx*>(mc.sm[0]);
+  fcx* sT = reinterpret_cast<fcx*>(mc.sm[1]);
+  fcx* sA = reinterpret_cast<fcx*>(mc.sm[2]);
+  fcx* sX = reinterpret_cast<fcx*>(mc.sm[3]);
+  int st = PF_OK;
+  Op<float> none = opN<float>(nullptr, 1);
+  for (int j = 1; j <= L + 1; ++j) {
+    const int dp = ext_dim(sys, j - 1), dj = ext_dim(sys, j);
+    const Op<float> V = vf(sys, q, j - 1);               // dp x dj
+    copy_in(sV, ld, V, dp, dj);                            // stage V (B operand)
+    row_gemm<float, S>(dp, dj, dp, opN<float>(mc.lu + (j - 1) * mat, ld), opN<float>(sV, ld),
+                       EpiStore<float>{sT, ld, mk<float>(1.f, 0.f)});      // T = g_{j-1} V
+    EpiShift<float> epi;
+    epi.c = sA;
+    epi.ld = ld;
+    epi.z = zD;
+    if (j <= L) {
+      epi.h = opN<float>(sys.fHd + ((size_t)q * L + (j - 1)) * sys.n * sys.n, sys.n);
+      epi.has_h = true;
+      epi.s = none;
+      epi.has_s = false;
+    } else {
+      epi.h = opN<float>(sys.fHR + (size_t)q * sys.nr * sys.nr, sys.nr);
+      epi.has_h = true;
+      epi.s = opN<float>(mc.fsr, ld);
+      epi.has_s = true;
+    }
+    row_gemm<float, S>(dj, dj, dp, opC<float>(sV, ld), opN<float>(sT, ld), epi);  // A_j - V^H T
+    st |= inverse(sA, ld, dj, mc.iwf);
+    copy_out(mc.lu + j * mat, ld, false, sA, ld, dj, dj);
+  }
+  // back substitution for the last block column
+  const int nr = sys.nr;
+  copy_out(sX, ld, false, mc.lu + (L + 1) * mat, ld, nr, nr);   // X_{L+1} = g_{L+1}
+  cvt_f_to_df(mc.xv + (L + 1) * mat, ld, sX, ld, nr, nr);
+  for (int j = L; j >= 0; --j) {
+    const int dj = ext_dim(sys, j), dn = ext_dim(sys, j + 1);
+    const Op<float> V = vf(sys, q, j);                   // dj x dn
+    row_gemm<float, S>(dj, nr, dn, V, opN<float>(sX, ld), EpiStore<float>{sT, ld, mk<float>(1.f, 0.f)});
+    row_gemm<float, S>(dj, nr, dj, opN<float>(mc.lu + j * mat, ld), opN<float>(sT, ld),
+                       EpiStore<float>{sX, ld, mk<float>(1.f, 0.f)});
+    cvt_f_to_df(mc.xv + j * mat, ld, sX, ld, dj, nr);
+  }
+  return st;
+}
+
+// ---------------------------------------------------------------------------
+// Stage 4: one refinement sweep (df64 residual, FP32 correction).
+// ---------------------------------------------------------------------------
+template <int S>
+__device__ void mixed_refine(const MCtx& mc, const MSys& sys, int q, dcx zL, dcx zD) {
+  const int ld = mc.ld, L = sys.L, nr = sys.nr;
+  const size_t mat = mc.mat;
+  // df64 window of X blocks (B operands) and FP32 work slots
+  dcx* xw[3] = {mc.sm[0], mc.sm[1], mc.sm[2]};
+  fcx* sR = reinterpret_cast<fcx*>(mc.sm[3]);
+  fcx* sYp = reinterpret_cast<fcx*>(mc.sm[4]);
+  fcx* sY = reinterpret_cast<fcx*>(mc.sm[5]);
+  dcx* R = mc.gs[M_R];
+  // window: xw[0] = X_{j-1}, xw[1] = X_j, xw[2] = X_{j+1}
+  copy_in(xw[1], ld, opN<df64>(mc.xv, ld), ext_dim(sys, 0), nr);
+  for (int j = 0; j <= L + 1; ++j) {
+    const int dj = ext_dim(sys, j);
+    if (j + 1 <= L + 1) copy_in(xw[2], ld, opN<df64>(mc.xv + (j + 1) * mat, ld), ext_dim(sys, j + 1), nr);
+    // r_j = b_j - z X_j + Hpart X_j + V_{j-1}^H X_{j-1} + V_j X_{j+1}
+    if (j == 0) {
+      row_gemm<df64, S>(dj, nr, dj, opN<df64>(mc.gs[M_ESL], ld), opN<df64>(xw[1], ld),
+                        EpiRes0{R, ld, xw[1], zL, false});
+    } else if (j <= L) {
+      row_gemm<df64, S>(dj, nr, dj, opN<df64>(sys.Hd + ((size_t)q * L + (j - 1)) * sys.n * sys.n, sys.n),
+                        opN<df64>(xw[1], ld), EpiRes0{R, ld, xw[1], zD, false});
+    } else {
+      row_gemm<df64, S>(dj, nr, dj, opN<df64>(sys.HR + (size_t)q * nr * nr, nr), opN<df64>(xw[1], ld),
+                        EpiRes0{R, ld, xw[1], zD, true});
+      row_gemm<df64, S>(dj, nr, dj, opN<df64>(mc.gs[M_SR], ld), opN<df64>(xw[1], ld), EpiAcc<df64>{R, ld});
+    }
+    if (j >= 1)
+      row_gemm<df64, S>(dj, nr, ext_dim(sys, j - 1), vd_h(sys, q, j - 1), opN<df64>(xw[0], ld),
+                        EpiAcc<df64>{R, ld});
+    if (j <= L)
+      row_gemm<df64, S>(dj, nr, ext_dim(sys, j + 1), vd(sys, q, j), opN<df64>(xw[2], ld), EpiAcc<df64>{R, ld});
+    cvt_df_to_f(sR, ld, false, R, ld, dj, nr);
+    // forward: y_j = g_j (r_j + V_{j-1}^H y_{j-1})
+    if (j >= 1)
+      row_gemm<float, S>(dj, nr, ext_dim(sys, j - 1), vf_h(sys, q, j - 1), opN<float>(sYp, ld),
+                         EpiStoreAddF{sR, ld, sR, ld});
+    row_gemm<float, S>(dj, nr, dj, opN<float>(mc.lu + j * mat, ld), opN<float>(sR, ld),
+                       EpiStoreAddF{sY, ld, nullptr, 0});
+    copy_out(mc.yv + j * mat, ld, false, sY, ld, dj, nr);
+    fcx* t = sYp;
+    sYp = sY;
+    sY = t;
+    dcx* u = xw[0];
+    xw[0] = xw[1];
+    xw[1] = xw[2];
+    xw[2] = u;
+  }
+  // backward: d_{L+1} = y_{L+1}; d_j = y_j + g_j V_j d_{j+1}; X += d
+  fcx* sD = sYp;   // holds y_{L+1}
+  fcx* sT = sR;
+  fcx* sN = sY;
+  {
+    dcx* x = mc.xv + (L + 1) * mat;
+    for (int i = threadIdx.x; i < nr * nr; i += blockDim.x) {
+      const int r = i % nr, c = i / nr;
+      const fcx v = sD[r + c * ld];
+      dcx xv = x[r + c * ld];
+      xv.x = xv.x + df64(v.x, 0.f);
+      xv.y = xv.y + df64(v.y, 0.f);
+      x[r + c * ld] = xv;
+    }
+    __syncthreads();
+  }
+  for (int j = L; j >= 0; --j) {
+    const int dj = ext_dim(sys, j), dn = ext_dim(sys, j + 1);
+    row_gemm<float, S>(dj, nr, dn, vf(sys, q, j), opN<float>(sD, ld), EpiStore<float>{sT, ld, mk<float>(1.f, 0.f)});
+    row_gemm<float, S>(dj, nr, dj, opN<float>(mc.lu + j * mat, ld), opN<float>(sT, ld),
+                       EpiCorr{sN, ld, mc.yv + j * mat, mc.xv + j * mat});
+    fcx* t = sD;
+    sD = sN;
+    sN = t;
+  }
+}
+
+// Stage 5: T_L = Re Tr[(X_0 Gamma_R)(X_0^H Gamma_L)] in df64.
+template <int S>
+__device__ double mixed_caroli(const MCtx& mc, const MSys& sys) {
+  const int ld = mc.ld, nl = sys.nl, nr = sys.nr;
+  dcx* sG = mc.sm[0];
+  dcx* sP = mc.sm[1];
+  dcx* sQ = mc.sm[2];
+  copy_in(sG, ld, opN<df64>(mc.gs[M_GMR], ld), nr, nr);
+  row_gemm<df64, S>(nl, nr, nr, opN<df64>(mc.xv, ld), opN<df64>(sG, ld), EpiStore<df64>{sP, ld, mk<df64>(1, 0)});
+  copy_in(sG, ld, opN<df64>(mc.gs[M_GML], ld), nl, nl);
+  row_gemm<df64, S>(nr, nl, nl, opC<df64>(mc.xv, ld), opN<df64>(sG, ld), EpiStore<df64>{sQ, ld, mk<df64>(1, 0)});
+  return trace_prod_re(sP, ld, opN<df64>(sQ, ld), nl, nr, mc.red);
+}
+
+}  // namespace pf

@@ -62,7 +62,7 @@ struct Ctx {
   cx<R>* gs[NG];
   int ld;  // odd leading dimension used for every working matrix
   InvWork<R> iw;
-  R* red;
+  double* red;
 };
 
 // ----------------------------------------------------------------------------
@@ -85,9 +85,9 @@ __device__ int decimate(const Ctx<R>& c, int m, cx<R> z, Op<R> h00, Op<R> a0, Op
   copy_in(es, ld, h00, m, m);
   copy_in(al, ld, a0, m, m);
   copy_in(be, ld, b0, m, m);
-  R maxdiff = max_abs(al, ld, m, m, c.red);
+  double maxdiff = max_abs(al, ld, m, m, c.red);
   int it = 0;
-  while (maxdiff > R(conv)) {
+  while (maxdiff > conv) {
     if (it >= max_iter) {
       st |= PF_NOT_CONVERGED;
       break;
@@ -183,7 +183,7 @@ __device__ int lead_pair(const Ctx<R>& c, const System<R>& sys, int q, double E,
 // Slots: SM0 = V, SM1 = T, SM2 = A (inverted), SM3 = g; G_W2 = G0N, G_W3 = U.
 // ----------------------------------------------------------------------------
 template <typename R, int S>
-__device__ int sweep_lr(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, R* trans) {
+__device__ int sweep_lr(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, double* trans) {
   const int ld = c.ld;
   const int n = sys.n, nl = sys.nl, nr = sys.nr, L = sys.L;
   cx<R>* V = c.sm[0];
@@ -240,7 +240,7 @@ __device__ int sweep_lr(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, 
 // Right-to-left sweep + Caroli T_R (lesser.f90:694-793).
 // ----------------------------------------------------------------------------
 template <typename R, int S>
-__device__ int sweep_rl(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, R* trans) {
+__device__ int sweep_rl(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, double* trans) {
   const int ld = c.ld;
   const int n = sys.n, nl = sys.nl, nr = sys.nr, L = sys.L;
   cx<R>* V = c.sm[0];

@@ -81,14 +81,20 @@ def _ptr(a, ctype=C.c_double):
 
 
 def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=None,
-                  zero_flag=None, max_iter=1000, want_transr=True, check=True):
+                  zero_flag=None, max_iter=1000, want_transr=True, check=True,
+                  precision="fp64", refine_iters=1):
     """Transmission for a batch of points through the host-pointer C entry.
 
     E: (npts,) energies (omega^2 for phonons).  blocks: TdbBlocks or dict.
     qidx: (npts,) q index into the stacked blocks (None: all 0).
     zero_flag: (npts,) nonzero -> T forced to 0 (the reference's ie == 1).
+    precision: "fp64" (pf_transport_tdb) or "mixed" (pf_transport_tdb_mixed:
+    double-float leads, FP32 factorisation, `refine_iters` double-float
+    refinement sweeps; T_L only).
     Returns dict(transl, transr, status, iters).
     """
+    if precision not in ("fp64", "mixed"):
+        raise ValueError("precision must be 'fp64' or 'mixed'")
     lib = _abi.load()
     if isinstance(blocks, dict):
         blocks = TdbBlocks.from_dict(blocks)
@@ -104,11 +110,17 @@ def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=No
     tr = np.zeros(npts)
     st = np.zeros(npts, dtype=np.int32)
     it = np.zeros((npts, 2), dtype=np.int32)
-    rc = lib.pf_transport_tdb(n, nl, nr, L, nq, *[_ptr(buf[k]) for k in BLOCK_NAMES], npts, _ptr(E),
-                              None if q is None else _ptr(q, C.c_int),
-                              None if z is None else _ptr(z, C.c_int),
-                              eta, eta0, dev_factor, convergence, max_iter, int(bool(want_transr)),
-                              _ptr(tl), _ptr(tr), _ptr(st, C.c_int), _ptr(it, C.c_int))
+    qp = None if q is None else _ptr(q, C.c_int)
+    zp = None if z is None else _ptr(z, C.c_int)
+    if precision == "fp64":
+        rc = lib.pf_transport_tdb(n, nl, nr, L, nq, *[_ptr(buf[k]) for k in BLOCK_NAMES], npts, _ptr(E),
+                                  qp, zp, eta, eta0, dev_factor, convergence, max_iter, int(bool(want_transr)),
+                                  _ptr(tl), _ptr(tr), _ptr(st, C.c_int), _ptr(it, C.c_int))
+    else:
+        want_transr = False
+        rc = lib.pf_transport_tdb_mixed(n, nl, nr, L, nq, *[_ptr(buf[k]) for k in BLOCK_NAMES], npts, _ptr(E),
+                                        qp, zp, eta, eta0, dev_factor, convergence, max_iter, int(refine_iters),
+                                        _ptr(tl), _ptr(st, C.c_int), _ptr(it, C.c_int))
     if rc != 0 and (check or rc != -4):
         _abi.check(rc)
     return dict(transl=tl, transr=tr if want_transr else None, status=st, iters=it)
@@ -123,7 +135,7 @@ class DeviceTransport:
     """
 
     def __init__(self, blocks, npts_max, *, eta, eta0, convergence, dev_factor=10.0,
-                 max_iter=1000, want_transr=False, device="cuda"):
+                 max_iter=1000, want_transr=False, device="cuda", precision="fp64", refine_iters=1):
         import torch
         self.torch = torch
         lib = _abi.load()
@@ -132,9 +144,18 @@ class DeviceTransport:
         nq, (n, nl, nr, L), arrs = blocks.stacked()
         self.dims = (n, nl, nr, L, nq)
         self.dev = {k: torch.from_numpy(fortran_block(v).copy()).to(device) for k, v in arrs.items()}
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = precision
+        self.refine_iters = int(refine_iters)
+        if precision == "mixed":
+            want_transr = False
         self.params = (eta, eta0, dev_factor, convergence, max_iter, int(bool(want_transr)))
         self.npts_max = npts_max
-        ws = lib.pf_transport_tdb_workspace_size(n, nl, nr, npts_max)
+        if precision == "fp64":
+            ws = lib.pf_transport_tdb_workspace_size(n, nl, nr, npts_max)
+        else:
+            ws = lib.pf_transport_tdb_mixed_workspace_size(n, nl, nr, L, nq, npts_max)
         if ws == 0:
             _abi.check(-3)
         self.work = torch.empty(ws, dtype=torch.uint8, device=device)
@@ -153,11 +174,19 @@ class DeviceTransport:
         s = stream if stream is not None else torch.cuda.current_stream()
         eta, eta0, dev_factor, conv, max_iter, want_transr = self.params
         d = self.dev
-        rc = lib.pf_transport_tdb_dev(
-            n, nl, nr, L, nq, *[d[k].data_ptr() for k in BLOCK_NAMES], npts, E.data_ptr(),
-            None if qidx is None else qidx.data_ptr(), None if zero_flag is None else zero_flag.data_ptr(),
-            eta, eta0, dev_factor, conv, max_iter, want_transr,
-            self.transl.data_ptr(), self.transr.data_ptr(), self.status.data_ptr(), self.iters.data_ptr(),
-            self.work.data_ptr(), self.work.numel(), C.c_void_p(s.cuda_stream))
+        qp = None if qidx is None else qidx.data_ptr()
+        zp = None if zero_flag is None else zero_flag.data_ptr()
+        if self.precision == "fp64":
+            rc = lib.pf_transport_tdb_dev(
+                n, nl, nr, L, nq, *[d[k].data_ptr() for k in BLOCK_NAMES], npts, E.data_ptr(), qp, zp,
+                eta, eta0, dev_factor, conv, max_iter, want_transr,
+                self.transl.data_ptr(), self.transr.data_ptr(), self.status.data_ptr(), self.iters.data_ptr(),
+                self.work.data_ptr(), self.work.numel(), C.c_void_p(s.cuda_stream))
+        else:
+            rc = lib.pf_transport_tdb_mixed_dev(
+                n, nl, nr, L, nq, *[d[k].data_ptr() for k in BLOCK_NAMES], npts, E.data_ptr(), qp, zp,
+                eta, eta0, dev_factor, conv, max_iter, self.refine_iters,
+                self.transl.data_ptr(), self.status.data_ptr(), self.iters.data_ptr(),
+                self.work.data_ptr(), self.work.numel(), C.c_void_p(s.cuda_stream))
         _abi.check(rc)
         return self.transl[:npts], self.transr[:npts], self.status[:npts]

@@ -1,0 +1,79 @@
+"""GPU accuracy of the mixed-precision path (double-float leads, FP32
+factorisation, double-float refinement) against the FP64 oracle, through
+the C ABI (pf_transport_tdb_mixed)."""
+import numpy as np
+import pytest
+
+from oracle import negf as N
+from phinfortran_gb300 import systems as S
+from phinfortran_gb300 import transport_tdb
+from tests.sisi_case import fp64_noise_floor, golden_close, sisi_blocks, sisi_params
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.abs(a - b) / np.maximum(np.abs(b), 1e-3)
+
+
+def test_mixed_sc_phonon_meets_1e8(cuda_ready):
+    b, E, p, _ = S.sc_phonon(ne=256)
+    Es = E[::8]
+    o = N.transport(Es, b, p["eta"], p["eta0"], p["convergence"], p["dev_factor"])
+    r0 = transport_tdb(Es, b, precision="mixed", refine_iters=0, **p)
+    r1 = transport_tdb(Es, b, precision="mixed", refine_iters=1, **p)
+    e0, e1 = rel(r0["transl"], o["transl"]), rel(r1["transl"], o["transl"])
+    assert (r1["status"] == 0).all()
+    # FP32 alone is ~1e-7; one double-float refinement sweep reaches < 1e-8 everywhere
+    assert np.median(e1) < np.median(e0) / 100
+    assert e1.max() <= 1e-8, e1.max()
+    # decimation iteration counts match the FP64 stopping rule
+    assert np.abs(r1["iters"][:, 0] - o["iters_left"]).max() <= 1
+
+
+def test_mixed_tb_ribbon_against_oracle(cuda_ready):
+    """Benchmark workload (n=32, L=200): error relative to the FP64 conditioning."""
+    b, E, p = S.tb_ribbon()
+    Es = E[::16]
+    r = transport_tdb(Es, b, precision="mixed", refine_iters=1, **p)
+    o, floor = fp64_noise_floor(Es, b, p)
+    d = np.abs(r["transl"] - o["transl"])
+    e = rel(r["transl"], o["transl"])
+    assert np.median(e) < 1e-8
+    # double-float carries ~2^-48 per operation (30x the FP64 unit roundoff):
+    # every point stays within 100x the point's FP64 perturbation floor
+    assert (d <= np.maximum(1e-8 * np.maximum(np.abs(o["transl"]), 1e-3), 100 * floor)).all()
+
+
+def test_mixed_sisi_against_reference_output(cuda_ready, sisi):
+    ik = 24
+    b = sisi_blocks(sisi, ik)
+    E = sisi["E"]
+    zf = np.zeros(E.size, np.int32)
+    zf[0] = 1
+    r = transport_tdb(E, b, precision="mixed", refine_iters=2, zero_flag=zf, **sisi_params(sisi))
+    ok, ad, q99 = golden_close(r["transl"], sisi["transl_tot"][:, ik], abs_tol=1e-6, rel_q99=1e-7)
+    assert ok, (ad, q99)
+    assert r["transl"][0] == 0.0
+
+
+def test_mixed_edge_shapes(cuda_ready):
+    """Uneven lead/device widths and a single device layer."""
+    rng = np.random.default_rng(7)
+    n, nl, nr = 6, 4, 5
+
+    def herm(m):
+        a = rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m))
+        return a + a.conj().T
+
+    for L in (1, 3):
+        Hd = np.array([herm(n) for _ in range(L)])
+        Hdv = rng.normal(size=(L - 1, n, n)) * 0.5
+        blocks = dict(HL=herm(nl), HLv=rng.normal(size=(nl, nl)) * 0.5, HR=herm(nr),
+                      HRv=rng.normal(size=(nr, nr)) * 0.5, Hd=Hd, Hdv=Hdv,
+                      Hld=rng.normal(size=(nl, n)) * 0.5, Hrd=rng.normal(size=(nr, n)) * 0.5)
+        E = np.linspace(-3, 3, 13)
+        r = transport_tdb(E, blocks, eta=0.0, eta0=1e-3, convergence=1e-12, dev_factor=1.0,
+                          precision="mixed", refine_iters=2)
+        o = N.transport(E, blocks, 0.0, 1e-3, 1e-12, 1.0)
+        assert np.abs(r["transl"] - o["transl"]).max() < 1e-9, L
