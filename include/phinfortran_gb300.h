@@ -78,11 +78,14 @@ int pf_version(void);
  * E[npts], qidx[npts] (may be NULL: all q = 0), zero_flag[npts] (may be
  * NULL) and the outputs transl[npts], transr[npts], status[npts],
  * iters[2*npts] (left, right iteration counts; may be NULL) are device
- * arrays.  work must hold pf_transport_tdb_workspace_size(n, nl, nr, npts)
- * bytes of device memory.  stream is a cudaStream_t (NULL: default stream).
+ * arrays.  work must hold pf_transport_tdb_workspace_size(n, nl, nr, nq,
+ * npts) bytes of device memory.  When the right lead blocks equal the left
+ * ones bitwise (HR == HL, HRv == HLv for a q), the right retarded surface
+ * function is taken as the adjoint of the left advanced one instead of a
+ * second decimation (exact identity for hermitian leads).  stream is a cudaStream_t (NULL: default stream).
  * The call is asynchronous on `stream`.
  */
-size_t pf_transport_tdb_workspace_size(int n, int nl, int nr, int npts);
+size_t pf_transport_tdb_workspace_size(int n, int nl, int nr, int nq, int npts);
 
 int pf_transport_tdb_dev(int n, int nl, int nr, int L, int nq,
                          const double* HL, const double* HLv,

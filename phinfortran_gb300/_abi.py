@@ -18,7 +18,7 @@ _ip = C.POINTER(C.c_int)
 SIGNATURES = {
     "pf_last_error": (C.c_char_p, []),
     "pf_version": (C.c_int, []),
-    "pf_transport_tdb_workspace_size": (C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int]),
+    "pf_transport_tdb_workspace_size": (C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     "pf_transport_tdb_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -31,10 +31,24 @@ using fcx = cx<float>;
 // Block set converted once per call: df64 copies (residual, leads, Caroli)
 // and FP32 copies (factorisation and corrections), same layout as the
 // FP64 input (column-major, ld = rows).
+// Row-compressed (ELL) copy of a block family: row r of block b keeps up to
+// K (column, value) pairs at [(b*rows + r)*K + k]; column -1 ends the row.
+struct Ell {
+  const int* col;
+  const dcx* val;
+  int K, rows;
+};
+
+enum { PF_ELL_K = 16 };
+
 struct MSys {
   int n, nl, nr, L, nq;
   const dcx *HL, *HLv, *HR, *HRv, *Hd, *Hdv, *Hld, *Hrd;
   const fcx *fHR, *fHd, *fHdv, *fHld, *fHrd;
+  // sparse copies for the residual: Hd, Hdv, Hdv^H, Hld, Hld^H, Hrd, Hrd^H;
+  // used when *ell_overflow == 0 (every row of every block has <= K nonzeros)
+  Ell eHd, eHdv, eHdvH, eHld, eHldH, eHrd, eHrdH;
+  const int* ell_overflow;
 };
 
 enum { NSM_M = 6 };
@@ -148,7 +162,13 @@ __device__ int mixed_leads(const MCtx& mc, const MSys& sys, int q, double E, con
     lead_sigma<df64, S>(c, nl, HLv);                            // SM1 = sl_adv
     gamma_from_sigma(mc.gs[M_GML], ld, c.sm[1], ld, nl, -1);
   }
-  {
+  if (P.lead_mirror && P.lead_mirror[q]) {
+    // identical leads: sr_ret = sl_adv^H, gmr_ret = -gml_adv (see lead_pair)
+    copy_out(mc.gs[M_SR], ld, true, c.sm[1], ld, nl, nl);
+    cvt_df_to_f(mc.fsr, ld, true, c.sm[1], ld, nl, nl);
+    copy_out(mc.gs[M_GMR], ld, false, mc.gs[M_GML], ld, nl, nl);
+    if (it_r) *it_r = *it_l;
+  } else {
     const dcx* HR = sys.HR + (size_t)q * nr * nr;
     const dcx* HRv = sys.HRv + (size_t)q * nr * nr;
     st |= decimate<df64, S>(c, nr, mk<df64>(df64(E), df64(eps)), opN<df64>(HR, nr), opC<df64>(HRv, nr),
@@ -241,6 +261,39 @@ __device__ int mixed_factor_solve(const MCtx& mc, const MSys& sys, int q, fcx zD
   return st;
 }
 
+// Accumulate acc += M(r,:) X(:,c) over the ELL row of M.
+__device__ __forceinline__ dcx ell_row_dot(const Ell& e, size_t blk, int r, const dcx* X, int ld, int c, dcx acc) {
+  const size_t base = (blk * e.rows + r) * (size_t)e.K;
+  for (int k = 0; k < e.K; ++k) {
+    const int cc = e.col[base + k];
+    if (cc < 0) break;
+    acc = cfma(e.val[base + k], X[cc + c * ld], acc);
+  }
+  return acc;
+}
+
+// Interior residual layer j (1..L) with sparse blocks, one pass:
+// R = - z X_j + Hd_j X_j + V_{j-1}^H X_{j-1} + V_j X_{j+1}
+__device__ void residual_sparse(const MSys& s, int q, int j, dcx zD, const dcx* Xm, const dcx* X0, const dcx* Xp,
+                                dcx* R, int ld) {
+  const int n = s.n, nr = s.nr, L = s.L;
+  for (int i = threadIdx.x; i < n * nr; i += blockDim.x) {
+    const int r = i / nr, c = i % nr;   // consecutive threads share the row: broadcast ELL loads
+    dcx acc = csub(czero<df64>(), cmul(zD, X0[r + c * ld]));
+    acc = ell_row_dot(s.eHd, (size_t)q * L + (j - 1), r, X0, ld, c, acc);
+    if (j == 1)
+      acc = ell_row_dot(s.eHldH, (size_t)q, r, Xm, ld, c, acc);
+    else
+      acc = ell_row_dot(s.eHdvH, (size_t)q * (L - 1) + (j - 2), r, Xm, ld, c, acc);
+    if (j == L)
+      acc = ell_row_dot(s.eHrdH, (size_t)q, r, Xp, ld, c, acc);
+    else
+      acc = ell_row_dot(s.eHdv, (size_t)q * (L - 1) + (j - 1), r, Xp, ld, c, acc);
+    R[r + c * ld] = acc;
+  }
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // Stage 4: one refinement sweep (df64 residual, FP32 correction).
 // ---------------------------------------------------------------------------
@@ -254,28 +307,33 @@ __device__ void mixed_refine(const MCtx& mc, const MSys& sys, int q, dcx zL, dcx
   fcx* sYp = reinterpret_cast<fcx*>(mc.sm[4]);
   fcx* sY = reinterpret_cast<fcx*>(mc.sm[5]);
   dcx* R = mc.gs[M_R];
+  const bool sparse = sys.ell_overflow != nullptr && *sys.ell_overflow == 0;
   // window: xw[0] = X_{j-1}, xw[1] = X_j, xw[2] = X_{j+1}
   copy_in(xw[1], ld, opN<df64>(mc.xv, ld), ext_dim(sys, 0), nr);
   for (int j = 0; j <= L + 1; ++j) {
     const int dj = ext_dim(sys, j);
     if (j + 1 <= L + 1) copy_in(xw[2], ld, opN<df64>(mc.xv + (j + 1) * mat, ld), ext_dim(sys, j + 1), nr);
     // r_j = b_j - z X_j + Hpart X_j + V_{j-1}^H X_{j-1} + V_j X_{j+1}
-    if (j == 0) {
-      row_gemm<df64, S>(dj, nr, dj, opN<df64>(mc.gs[M_ESL], ld), opN<df64>(xw[1], ld),
-                        EpiRes0{R, ld, xw[1], zL, false});
-    } else if (j <= L) {
-      row_gemm<df64, S>(dj, nr, dj, opN<df64>(sys.Hd + ((size_t)q * L + (j - 1)) * sys.n * sys.n, sys.n),
-                        opN<df64>(xw[1], ld), EpiRes0{R, ld, xw[1], zD, false});
+    if (j >= 1 && j <= L && sparse) {
+      residual_sparse(sys, q, j, zD, xw[0], xw[1], xw[2], R, ld);
     } else {
-      row_gemm<df64, S>(dj, nr, dj, opN<df64>(sys.HR + (size_t)q * nr * nr, nr), opN<df64>(xw[1], ld),
-                        EpiRes0{R, ld, xw[1], zD, true});
-      row_gemm<df64, S>(dj, nr, dj, opN<df64>(mc.gs[M_SR], ld), opN<df64>(xw[1], ld), EpiAcc<df64>{R, ld});
+      if (j == 0) {
+        row_gemm<df64, S>(dj, nr, dj, opN<df64>(mc.gs[M_ESL], ld), opN<df64>(xw[1], ld),
+                          EpiRes0{R, ld, xw[1], zL, false});
+      } else if (j <= L) {
+        row_gemm<df64, S>(dj, nr, dj, opN<df64>(sys.Hd + ((size_t)q * L + (j - 1)) * sys.n * sys.n, sys.n),
+                          opN<df64>(xw[1], ld), EpiRes0{R, ld, xw[1], zD, false});
+      } else {
+        row_gemm<df64, S>(dj, nr, dj, opN<df64>(sys.HR + (size_t)q * nr * nr, nr), opN<df64>(xw[1], ld),
+                          EpiRes0{R, ld, xw[1], zD, true});
+        row_gemm<df64, S>(dj, nr, dj, opN<df64>(mc.gs[M_SR], ld), opN<df64>(xw[1], ld), EpiAcc<df64>{R, ld});
+      }
+      if (j >= 1)
+        row_gemm<df64, S>(dj, nr, ext_dim(sys, j - 1), vd_h(sys, q, j - 1), opN<df64>(xw[0], ld),
+                          EpiAcc<df64>{R, ld});
+      if (j <= L)
+        row_gemm<df64, S>(dj, nr, ext_dim(sys, j + 1), vd(sys, q, j), opN<df64>(xw[2], ld), EpiAcc<df64>{R, ld});
     }
-    if (j >= 1)
-      row_gemm<df64, S>(dj, nr, ext_dim(sys, j - 1), vd_h(sys, q, j - 1), opN<df64>(xw[0], ld),
-                        EpiAcc<df64>{R, ld});
-    if (j <= L)
-      row_gemm<df64, S>(dj, nr, ext_dim(sys, j + 1), vd(sys, q, j), opN<df64>(xw[2], ld), EpiAcc<df64>{R, ld});
     cvt_df_to_f(sR, ld, false, R, ld, dj, nr);
     // forward: y_j = g_j (r_j + V_{j-1}^H y_{j-1})
     if (j >= 1)

@@ -15,7 +15,7 @@
 #include <vector>
 
 #include "../../include/phinfortran_gb300.h"
-#include "mixed.cuh"
+#include "warp_engine.cuh"
 
 using pf::cx;
 
@@ -125,6 +125,25 @@ __global__ void __launch_bounds__(kThreads) transport_kernel(pf::System<R> sys, 
   }
 }
 
+// mirror[q] = 1 when the right lead blocks equal the left ones bitwise.
+__global__ void lead_mirror_kernel(const double* HL, const double* HLv, const double* HR, const double* HRv,
+                                   int m2, int nq, int* mirror) {
+  // m2 = 2 * nl * nl doubles per block; one CTA per q
+  const int q = blockIdx.x;
+  if (q >= nq) return;
+  __shared__ int diff;
+  if (threadIdx.x == 0) diff = 0;
+  __syncthreads();
+  const size_t off = (size_t)q * m2;
+  int d = 0;
+  for (int i = threadIdx.x; i < m2; i += blockDim.x)
+    d |= (__double_as_longlong(HL[off + i]) != __double_as_longlong(HR[off + i])) |
+         (__double_as_longlong(HLv[off + i]) != __double_as_longlong(HRv[off + i]));
+  if (d) atomicOr(&diff, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) mirror[q] = diff ? 0 : 1;
+}
+
 struct DevInfo {
   int sms = 0;
   size_t smem_optin = 0;
@@ -172,26 +191,39 @@ int launch_transport(const pf::System<R>& sys, const pf::Points& pts, const pf::
   const int S = (lay.m + 31) / 32;
   int grid = (S == 1) ? grid_for<R, 1>(lay, pts.npts) : grid_for<R, 2>(lay, pts.npts);
   if (grid <= 0) return set_err(PF_ERR_SIZE, "pf: kernel does not fit on the device");
-  const size_t need = 256 + (size_t)grid * lay.per_cta_bytes;
+  const size_t mir = ((size_t)sys.nq * sizeof(int) + 255) & ~(size_t)255;
+  const size_t need = 256 + mir + (size_t)grid * lay.per_cta_bytes;
   if (!work || work_bytes < need) return set_err(PF_ERR_ARG, "pf: workspace too small");
   int* queue = reinterpret_cast<int*>(work);
-  char* gscr = reinterpret_cast<char*>(work) + 256;
+  int* mirror = reinterpret_cast<int*>(reinterpret_cast<char*>(work) + 256);
+  char* gscr = reinterpret_cast<char*>(work) + 256 + mir;
   PF_CUDA(cudaMemsetAsync(queue, 0, sizeof(int), stream));
+  pf::Params P2 = P;
+  if (sys.nl == sys.nr) {
+    lead_mirror_kernel<<<sys.nq, 256, 0, stream>>>(reinterpret_cast<const double*>(sys.HL),
+                                                   reinterpret_cast<const double*>(sys.HLv),
+                                                   reinterpret_cast<const double*>(sys.HR),
+                                                   reinterpret_cast<const double*>(sys.HRv), 2 * sys.nl * sys.nl,
+                                                   sys.nq, mirror);
+    P2.lead_mirror = mirror;
+  } else {
+    P2.lead_mirror = nullptr;
+  }
   if (S == 1)
-    transport_kernel<R, 1><<<grid, kThreads, lay.smem, stream>>>(sys, pts, P, out, lay, gscr, queue);
+    transport_kernel<R, 1><<<grid, kThreads, lay.smem, stream>>>(sys, pts, P2, out, lay, gscr, queue);
   else
-    transport_kernel<R, 2><<<grid, kThreads, lay.smem, stream>>>(sys, pts, P, out, lay, gscr, queue);
+    transport_kernel<R, 2><<<grid, kThreads, lay.smem, stream>>>(sys, pts, P2, out, lay, gscr, queue);
   PF_CUDA(cudaGetLastError());
   return PF_SUCCESS;
 }
 
 template <typename R>
-size_t workspace_bytes(int n, int nl, int nr, int npts) {
+size_t workspace_bytes(int n, int nl, int nr, int nq, int npts) {
   const Layout lay = make_layout<R>(n, nl, nr);
   const int S = (lay.m + 31) / 32;
   int grid = (S == 1) ? grid_for<R, 1>(lay, npts > 0 ? npts : 1) : grid_for<R, 2>(lay, npts > 0 ? npts : 1);
   if (grid <= 0) return 0;
-  return 256 + (size_t)grid * lay.per_cta_bytes;
+  return 256 + (((size_t)nq * sizeof(int) + 255) & ~(size_t)255) + (size_t)grid * lay.per_cta_bytes;
 }
 
 pf::System<double> make_sys(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
@@ -242,12 +274,43 @@ __global__ void convert_blocks_kernel(const cx<double>* src, dcx* d, fcx* f, siz
   }
 }
 
+// ELL copy of `count` blocks (rows x cols each, column-major).  With
+// `ct` the ELL describes the conjugate transpose (rows of M^H = columns of M).
+// One thread per output row; rows with more than K nonzeros set *overflow.
+__global__ void build_ell_kernel(const dcx* M, int rows, int cols, int count, int ct, int K, int* col_out,
+                                 dcx* val_out, int* overflow) {
+  const int orows = ct ? cols : rows, ocols = ct ? rows : cols;
+  const size_t total = (size_t)count * orows;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t b = t / orows;
+    const int r = (int)(t % orows);
+    const dcx* Mb = M + b * (size_t)rows * cols;
+    int k = 0;
+    for (int c = 0; c < ocols; ++c) {
+      dcx v = ct ? Mb[c + (size_t)r * rows] : Mb[r + (size_t)c * rows];
+      if (ct) v = pf::cconj(v);
+      const bool nz = v.x.hi != 0.f || v.x.lo != 0.f || v.y.hi != 0.f || v.y.lo != 0.f;
+      if (!nz) continue;
+      if (k < K) {
+        col_out[t * K + k] = c;
+        val_out[t * K + k] = v;
+      } else {
+        atomicOr(overflow, 1);
+      }
+      ++k;
+    }
+    for (; k < K; ++k) col_out[t * K + k] = -1;
+  }
+}
+
 struct MixedLayout {
   Layout base;     // smem slots are df64-sized (16 B per complex)
   size_t smem;
   size_t per_cta;  // bytes of per-CTA scratch
   size_t blocks_d, blocks_f;  // bytes of converted block copies (per call)
   size_t cnt[8];   // complex elements per block family (all q)
+  size_t ell_rows[7];  // ELL rows: Hd, Hdv, Hdv^H, Hld, Hld^H, Hrd, Hrd^H
+  size_t ell_bytes;
 };
 
 MixedLayout make_mixed_layout(int n, int nl, int nr, int L, int nq) {
@@ -270,6 +333,15 @@ MixedLayout make_mixed_layout(int n, int nl, int nr, int L, int nq) {
   size_t totf = 0;
   for (int i = 2; i < 8; ++i) totf += (c[i] * 8 + 255) & ~(size_t)255;  // HR, HRv(unused), Hd, Hdv, Hld, Hrd
   m.blocks_f = totf;
+  const size_t er[7] = {(size_t)nq * L * n, (size_t)nq * (L > 1 ? L - 1 : 0) * n,
+                        (size_t)nq * (L > 1 ? L - 1 : 0) * n, (size_t)nq * nl, (size_t)nq * n, (size_t)nq * nr,
+                        (size_t)nq * n};
+  size_t eb = 256;  // overflow flag
+  for (int i = 0; i < 7; ++i) {
+    m.ell_rows[i] = er[i];
+    eb += ((er[i] * pf::PF_ELL_K * 4 + 255) & ~(size_t)255) + ((er[i] * pf::PF_ELL_K * 16 + 255) & ~(size_t)255);
+  }
+  m.ell_bytes = eb + (((size_t)nq * sizeof(int) + 255) & ~(size_t)255);  // + lead mirror flags
   return m;
 }
 
@@ -337,6 +409,346 @@ __global__ void __launch_bounds__(kThreads) mixed_kernel(pf::MSys sys, pf::Point
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Mixed path, cross-sections <= 32: leads kernel (CTA per point) + layer
+// kernel (warp per point).
+// ---------------------------------------------------------------------------
+constexpr int kWarpsPerCta = 8;
+
+// Copy an (m x m) df64/FP32 matrix from scratch (ld) into a padded 32x32
+// per-point block (ld 32); `ident` puts ones on the padded diagonal.
+template <typename T>
+__device__ void pad_store(T* dst, const T* src, int ld, int m, bool ident) {
+  for (int i = threadIdx.x; i < pf::wp::NW * pf::wp::NW; i += blockDim.x) {
+    const int r = i % pf::wp::NW, c = i / pf::wp::NW;
+    T v;
+    v.x = decltype(v.x)(0.f, 0.f);
+    v.y = decltype(v.y)(0.f, 0.f);
+    if (r < m && c < m) v = src[r + c * ld];
+    dst[i] = v;
+  }
+}
+__device__ void pad_store_f(fcx* dst, const fcx* src, int ld, int m, bool ident) {
+  for (int i = threadIdx.x; i < pf::wp::NW * pf::wp::NW; i += blockDim.x) {
+    const int r = i % pf::wp::NW, c = i / pf::wp::NW;
+    fcx v = pf::mk<float>(0.f, 0.f);
+    if (r < m && c < m)
+      v = src[r + c * ld];
+    else if (ident && r == c)
+      v = pf::mk<float>(1.f, 0.f);
+    dst[i] = v;
+  }
+}
+
+template <int S>
+__global__ void __launch_bounds__(kThreads) leads_kernel(pf::MSys sys, pf::Points pts, pf::Params P,
+                                                         pf::Outputs out, MixedLayout lay, size_t per_cta,
+                                                         char* scratch, pf::wp::LeadOut lo, int* lead_status,
+                                                         int* queue) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  pf::MCtx c;
+  const size_t mat = lay.base.mat;
+  dcx* s = reinterpret_cast<dcx*>(smem_raw);
+  for (int i = 0; i < pf::NSM_M; ++i) c.sm[i] = s + i * mat;
+  unsigned char* tail = reinterpret_cast<unsigned char*>(s + pf::NSM_M * mat);
+  c.red = reinterpret_cast<double*>(tail);
+  c.iwd.rowk = reinterpret_cast<dcx*>(tail + 32 * sizeof(double));
+  c.iwd.colk = c.iwd.rowk + lay.base.m;
+  int* ip = reinterpret_cast<int*>(c.iwd.colk + lay.base.m);
+  c.iwd.perm = ip;
+  c.iwd.flag = ip + lay.base.m;
+  c.iwf.rowk = reinterpret_cast<fcx*>(c.iwd.rowk);
+  c.iwf.colk = reinterpret_cast<fcx*>(c.iwd.colk);
+  c.iwf.perm = c.iwd.perm;
+  c.iwf.flag = c.iwd.flag;
+  char* base = scratch + (size_t)blockIdx.x * per_cta;
+  dcx* g = reinterpret_cast<dcx*>(base);
+  for (int i = 0; i < pf::NGM; ++i) c.gs[i] = g + i * mat;
+  // lu/fsr of the CTA scratch hold g_0 and Sigma_R before they are padded out
+  c.xv = g + pf::NGM * mat;
+  c.lu = reinterpret_cast<fcx*>(c.xv);
+  c.yv = c.lu + mat;
+  c.fsr = c.yv + mat;
+  c.ld = lay.base.ld;
+  c.mat = mat;
+  __shared__ int s_p;
+  const size_t B = (size_t)pf::wp::NW * pf::wp::NW;
+  for (;;) {
+    if (threadIdx.x == 0) s_p = atomicAdd(queue, 1);
+    __syncthreads();
+    const int p = s_p;
+    __syncthreads();
+    if (p >= pts.npts) break;
+    const int q = pts.qidx ? pts.qidx[p] : 0;
+    int itl = 0, itr = 0;
+    const int st = pf::mixed_leads<S>(c, sys, q, pts.E[p], P, &itl, &itr);
+    pad_store_f(lo.g0 + p * B, c.lu, c.ld, sys.nl, true);
+    pad_store_f(lo.fsr + p * B, c.fsr, c.ld, sys.nr, false);
+    pad_store(lo.esl + p * B, c.gs[pf::M_ESL], c.ld, sys.nl, false);
+    pad_store(lo.sr + p * B, c.gs[pf::M_SR], c.ld, sys.nr, false);
+    pad_store(lo.gml + p * B, c.gs[pf::M_GML], c.ld, sys.nl, false);
+    pad_store(lo.gmr + p * B, c.gs[pf::M_GMR], c.ld, sys.nr, false);
+    if (threadIdx.x == 0) {
+      lead_status[p] = st;
+      if (out.iters) {
+        out.iters[2 * p] = itl;
+        out.iters[2 * p + 1] = itr;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+
+// Refinement residual of every point and every extended layer in parallel:
+// r_j = b_j - A X (df64), written in FP32 into the forward-vector slab
+// (the forward pass consumes r_j before it overwrites the slot with y_j).
+// One thread per element; lanes run along the rows of one column.
+__device__ __forceinline__ dcx ell_acc(const pf::Ell& e, size_t blk, int r, const dcx* X, int c, dcx acc) {
+  const size_t base = (blk * e.rows + r) * (size_t)e.K;
+  for (int k = 0; k < e.K; ++k) {
+    const int cc = e.col[base + k];
+    if (cc < 0) break;
+    acc = pf::cfma(e.val[base + k], X[cc + c * pf::wp::NW], acc);
+  }
+  return acc;
+}
+__device__ __forceinline__ dcx dense_acc(const dcx* M, int ldm, int kdim, bool ct, int r, const dcx* X, int c,
+                                         dcx acc) {
+  for (int k = 0; k < kdim; ++k) {
+    const dcx m = ct ? pf::cconj(M[k + (size_t)r * ldm]) : M[r + (size_t)k * ldm];
+    acc = pf::cfma(m, X[k + c * pf::wp::NW], acc);
+  }
+  return acc;
+}
+
+__global__ void residual_kernel(pf::MSys s, pf::Points pts, pf::Params P, pf::wp::LeadOut lo, pf::wp::Slabs sl) {
+  const int NW = pf::wp::NW;
+  const size_t B = (size_t)NW * NW;
+  const int L = s.L, n = s.n;
+  const size_t per_pt = (size_t)(L + 2) * B;
+  const size_t total = (size_t)pts.npts * per_pt;
+  const bool sparse = s.ell_overflow != nullptr && *s.ell_overflow == 0;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(idx % NW);
+    const int c = (int)((idx / NW) % NW);
+    const int j = (int)((idx / B) % (L + 2));
+    const int p = (int)(idx / per_pt);
+    const int dj = j == 0 ? s.nl : (j == L + 1 ? s.nr : n);
+    fcx outv = pf::mk<float>(0.f, 0.f);
+    if (r < dj && c < s.nr) {
+      const int q = pts.qidx ? pts.qidx[p] : 0;
+      const double E = pts.E[p];
+      const double eps = E * P.eta + P.eta0;
+      const dcx z = pf::mk<pf::df64>(pf::df64(E), pf::df64((j == 0 ? 1.0 : P.dev_factor) * eps));
+      const dcx* xb = sl.xv + (size_t)p * per_pt;
+      const dcx* X0 = xb + (size_t)j * B;
+      dcx acc = pf::csub(pf::wp::dz(), pf::cmul(z, X0[r + c * NW]));
+      if (j == L + 1 && r == c) acc.x = acc.x + pf::df64(1.f, 0.f);
+      if (j == 0) {
+        acc = dense_acc(lo.esl + (size_t)p * B, NW, s.nl, false, r, X0, c, acc);
+        const dcx* Xp = xb + B;
+        acc = sparse ? ell_acc(s.eHld, (size_t)q, r, Xp, c, acc)
+                     : dense_acc(s.Hld + (size_t)q * s.nl * n, s.nl, n, false, r, Xp, c, acc);
+      } else if (j <= L) {
+        const dcx* Xm = xb + (size_t)(j - 1) * B;
+        const dcx* Xp = xb + (size_t)(j + 1) * B;
+        if (sparse) {
+          acc = ell_acc(s.eHd, (size_t)q * L + (j - 1), r, X0, c, acc);
+          acc = (j == 1) ? ell_acc(s.eHldH, (size_t)q, r, Xm, c, acc)
+                         : ell_acc(s.eHdvH, (size_t)q * (L - 1) + (j - 2), r, Xm, c, acc);
+          acc = (j == L) ? ell_acc(s.eHrdH, (size_t)q, r, Xp, c, acc)
+                         : ell_acc(s.eHdv, (size_t)q * (L - 1) + (j - 1), r, Xp, c, acc);
+        } else {
+          acc = dense_acc(s.Hd + ((size_t)q * L + (j - 1)) * n * n, n, n, false, r, X0, c, acc);
+          acc = (j == 1) ? dense_acc(s.Hld + (size_t)q * s.nl * n, s.nl, s.nl, true, r, Xm, c, acc)
+                         : dense_acc(s.Hdv + ((size_t)q * (L - 1) + (j - 2)) * n * n, n, n, true, r, Xm, c, acc);
+          acc = (j == L) ? dense_acc(s.Hrd + (size_t)q * s.nr * n, s.nr, s.nr, true, r, Xp, c, acc)
+                         : dense_acc(s.Hdv + ((size_t)q * (L - 1) + (j - 1)) * n * n, n, n, false, r, Xp, c, acc);
+        }
+      } else {
+        const dcx* Xm = xb + (size_t)L * B;
+        acc = dense_acc(s.HR + (size_t)q * s.nr * s.nr, s.nr, s.nr, false, r, X0, c, acc);
+        acc = dense_acc(lo.sr + (size_t)p * B, NW, s.nr, false, r, X0, c, acc);
+        acc = sparse ? ell_acc(s.eHrd, (size_t)q, r, Xm, c, acc)
+                     : dense_acc(s.Hrd + (size_t)q * s.nr * n, s.nr, n, false, r, Xm, c, acc);
+      }
+      outv = pf::mk<float>(acc.x.hi, acc.y.hi);
+    }
+    sl.yv[idx] = outv;
+  }
+}
+
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 1)
+    layer_kernel(pf::MSys sys, pf::Points pts, pf::Params P, int phase, pf::Outputs out, pf::wp::LeadOut lo,
+                 pf::wp::Slabs sl, int* lead_status, int* queue) {
+  using namespace pf::wp;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  fcx* G = reinterpret_cast<fcx*>(smem_raw) + (size_t)w * 2 * LDW * NW;
+  fcx* Vb = G + LDW * NW;
+  const int L = sys.L, nr = sys.nr;
+  const size_t B = (size_t)NW * NW;
+  for (;;) {
+    int p = 0;
+    if (lane == 0) p = atomicAdd(queue, 1);
+    p = __shfl_sync(0xffffffffu, p, 0);
+    if (p >= pts.npts) break;
+    const int q = pts.qidx ? pts.qidx[p] : 0;
+    const double E = pts.E[p];
+    const double eps = E * P.eta + P.eta0;
+    const fcx zf = pf::mk<float>((float)E, (float)(P.dev_factor * eps));
+    int st = lead_status[p];
+    const bool do_factor = (phase == 0), do_refine = (phase == 1), do_caroli = (phase == 2);
+    fcx* lu = sl.lu + (size_t)p * (L + 2) * B;
+    fcx* yv = sl.yv + (size_t)p * (L + 2) * B;
+    dcx* xv = sl.xv + (size_t)p * (L + 2) * B;
+    fcx a[NW], t[NW], u[NW];
+    if (do_factor) {
+    // ---- g_0 = gl (padded), kept in G and lu[0]
+    load_col(lo.g0 + p * B, NW, NW, NW, false, lane, a);
+    store_col_smem(G, lane, a);
+#pragma unroll
+    for (int r = 0; r < NW; ++r) lu[r + lane * NW] = a[r];
+    __syncwarp();
+    // ---- FP32 block LU, j = 1..L+1
+    for (int j = 1; j <= L + 1; ++j) {
+      const int dj = edim(sys, j);
+      stage_v(Vb, vview(sys, q, j - 1), lane);
+#pragma unroll
+      for (int r = 0; r < NW; ++r) a[r] = Vb[r + lane * LDW];
+      wgemm(G, a, t);                          // T = g_{j-1} V
+      wgemm_ct(Vb, t, u);                      // S = V^H T
+      const fcx* H = (j <= L) ? sys.fHd + ((size_t)q * L + (j - 1)) * sys.n * sys.n : sys.fHR + (size_t)q * nr * nr;
+      const int ldh = (j <= L) ? sys.n : nr;
+      const fcx* Sr = lo.fsr + p * B;
+#pragma unroll
+      for (int r = 0; r < NW; ++r) {
+        fcx v;
+        if (r < dj && lane < dj) {
+          v = pf::mk<float>(-u[r].x, -u[r].y);
+          if (r == lane) v = pf::cadd(v, zf);
+          v = pf::csub(v, H[r + (size_t)lane * ldh]);
+          if (j == L + 1) v = pf::csub(v, Sr[r + lane * NW]);
+        } else {
+          v = pf::mk<float>(r == lane ? 1.f : 0.f, 0.f);
+        }
+        a[r] = v;
+      }
+      __syncwarp();
+      store_col_smem(G, lane, a);
+      __syncwarp();
+      st |= winverse(G, Vb, lu + (size_t)j * B, lane);
+      fcx* tmp = G;
+      G = Vb;
+      Vb = tmp;
+    }
+    // ---- back substitution: X_{L+1} = g_{L+1}; X_j = g_j V_j X_{j+1}
+#pragma unroll
+    for (int r = 0; r < NW; ++r) a[r] = (lane < nr) ? G[r + lane * LDW] : fz();
+#pragma unroll
+    for (int r = 0; r < NW; ++r)
+      xv[(size_t)(L + 1) * B + r + lane * NW] = pf::mk<pf::df64>(pf::df64(a[r].x, 0.f), pf::df64(a[r].y, 0.f));
+    for (int j = L; j >= 0; --j) {
+      __syncwarp();
+      stage_v(Vb, vview(sys, q, j), lane);
+      wgemm(Vb, a, t);                         // W = V_j X_{j+1}
+      __syncwarp();
+      load_col(lu + (size_t)j * B, NW, NW, NW, false, lane, u);
+      store_col_smem(G, lane, u);
+      __syncwarp();
+      wgemm(G, t, a);                          // X_j = g_j W
+#pragma unroll
+      for (int r = 0; r < NW; ++r) {
+        if (lane >= nr) a[r] = fz();
+        xv[(size_t)j * B + r + lane * NW] = pf::mk<pf::df64>(pf::df64(a[r].x, 0.f), pf::df64(a[r].y, 0.f));
+      }
+    }
+    }  // do_factor
+    // ---- one refinement sweep (the residual r_j was written into yv[j] by residual_kernel)
+    if (do_refine) {
+      // forward: y_j = g_j (r_j + V_{j-1}^H y_{j-1})
+      for (int j = 0; j <= L + 1; ++j) {
+        __syncwarp();
+        load_col(yv + (size_t)j * B, NW, NW, NW, false, lane, u);
+        if (j >= 1) {
+          stage_v(Vb, vview(sys, q, j - 1), lane);
+          wgemm_ct(Vb, a, t);                  // a holds y_{j-1}
+#pragma unroll
+          for (int r = 0; r < NW; ++r) u[r] = pf::cadd(u[r], t[r]);
+        }
+        __syncwarp();
+        load_col(lu + (size_t)j * B, NW, NW, NW, false, lane, t);
+        store_col_smem(G, lane, t);
+        __syncwarp();
+        wgemm(G, u, a);                        // y_j
+#pragma unroll
+        for (int r = 0; r < NW; ++r) yv[(size_t)j * B + r + lane * NW] = a[r];
+      }
+      // backward: d_{L+1} = y_{L+1}; d_j = y_j + g_j V_j d_{j+1}; X += d
+#pragma unroll
+      for (int r = 0; r < NW; ++r) {
+        dcx& x = xv[(size_t)(L + 1) * B + r + lane * NW];
+        x.x = x.x + pf::df64(a[r].x, 0.f);
+        x.y = x.y + pf::df64(a[r].y, 0.f);
+      }
+      for (int j = L; j >= 0; --j) {
+        __syncwarp();
+        stage_v(Vb, vview(sys, q, j), lane);
+        wgemm(Vb, a, t);
+        __syncwarp();
+        load_col(lu + (size_t)j * B, NW, NW, NW, false, lane, u);
+        store_col_smem(G, lane, u);
+        __syncwarp();
+        wgemm(G, t, a);
+#pragma unroll
+        for (int r = 0; r < NW; ++r) {
+          a[r] = pf::cadd(a[r], yv[(size_t)j * B + r + lane * NW]);
+          dcx& x = xv[(size_t)j * B + r + lane * NW];
+          x.x = x.x + pf::df64(a[r].x, 0.f);
+          x.y = x.y + pf::df64(a[r].y, 0.f);
+        }
+      }
+    }
+    if (do_factor) {
+      if (lane == 0) lead_status[p] = st;
+      continue;
+    }
+    if (do_refine) continue;
+    // ---- Caroli in df64: lane c: P[:,c] = X0 GR[:,c]; Q[c,:] = X0[:,c]^H GL; tr += sum_r P[r,c] Q[c,r]
+    double tr = 0.0;
+    if (do_caroli) {
+      const dcx* X0 = xv;
+      const dcx* GR = lo.gmr + p * B;
+      const dcx* GL = lo.gml + p * B;
+      const int nl = sys.nl;
+      if (lane < nr) {
+        pf::df64 acc(0.f, 0.f);
+        for (int r = 0; r < nl; ++r) {
+          dcx pr = pf::wp::dz();
+          for (int k = 0; k < nr; ++k) pr = pf::cfma(X0[r + k * NW], GR[k + lane * NW], pr);
+          dcx qr = pf::wp::dz();
+          for (int k = 0; k < nl; ++k) qr = pf::cfma(pf::cconj(X0[k + lane * NW]), GL[k + r * NW], qr);
+          acc = acc + (pr.x * qr.x - pr.y * qr.y);
+        }
+        tr = pf::to_d(acc);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
+    }
+    if (lane == 0) {
+      const bool zero = pts.zero_flag && pts.zero_flag[p];
+      double v = tr;
+      if (zero || v < 1.0e-60) v = 0.0;
+      if (!(v == v)) st |= pf::PF_NAN;
+      out.transl[p] = v;
+      out.status[p] = st;
+    }
+  }
+}
+
 template <int S>
 int mixed_grid(const MixedLayout& lay, int npts) {
   auto k = mixed_kernel<S>;
@@ -349,12 +761,82 @@ int mixed_grid(const MixedLayout& lay, int npts) {
   return g < npts ? g : npts;
 }
 
-size_t mixed_workspace_bytes(int n, int nl, int nr, int L, int nq, int npts) {
-  MixedLayout lay = make_mixed_layout(n, nl, nr, L, nq);
+// Workspace plan of the mixed path (byte offsets into the caller's buffer).
+struct MixedPlan {
+  MixedLayout lay;
+  bool warp_engine;     // cross-sections <= 32: leads kernel + warp-per-point layer kernel
+  int grid_a, grid_b;   // CTA counts of the (leads / fused) kernel and the layer kernel
+  size_t per_cta_a;     // per-CTA scratch of kernel A
+  size_t off_blocks, off_ell, off_scratch, off_lead, off_lstat, off_slabs, total;
+  size_t smem_b;
+};
+
+size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+template <int S>
+int leads_grid(const MixedLayout& lay, int npts) {
+  auto k = leads_kernel<S>;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.smem) != cudaSuccess) return -1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, lay.smem) != cudaSuccess) return -1;
+  if (per_sm < 1) return -1;
+  DevInfo d = device_info();
+  int g = d.sms * per_sm;
+  return g < npts ? g : npts;
+}
+
+bool make_plan(int n, int nl, int nr, int L, int nq, int npts, MixedPlan& P) {
+  P.lay = make_mixed_layout(n, nl, nr, L, nq);
+  const MixedLayout& lay = P.lay;
   const int S = (lay.base.m + 31) / 32;
-  const int g = (S == 1) ? mixed_grid<1>(lay, npts > 0 ? npts : 1) : mixed_grid<2>(lay, npts > 0 ? npts : 1);
-  if (g <= 0) return 0;
-  return 256 + lay.blocks_d + lay.blocks_f + (size_t)g * lay.per_cta;
+  const int np = npts > 0 ? npts : 1;
+  P.warp_engine = lay.base.m <= pf::wp::NW;
+  const size_t Bn = (size_t)pf::wp::NW * pf::wp::NW;
+  if (P.warp_engine) {
+    P.grid_a = leads_grid<1>(lay, np);
+    P.per_cta_a = al256((size_t)pf::NGM * lay.base.mat * 16 + 3 * lay.base.mat * 8);
+    P.smem_b = (size_t)kWarpsPerCta * 2 * pf::wp::LDW * pf::wp::NW * 8;
+    if (cudaFuncSetAttribute(layer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem_b) !=
+        cudaSuccess)
+      return false;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, layer_kernel, kWarpsPerCta * 32, P.smem_b) !=
+            cudaSuccess ||
+        per_sm < 1)
+      return false;
+    DevInfo d = device_info();
+    const int warps = (np + 0);
+    int gb = d.sms * per_sm;
+    const int need_ctas = (warps + kWarpsPerCta - 1) / kWarpsPerCta;
+    P.grid_b = gb < need_ctas ? gb : need_ctas;
+  } else {
+    P.grid_a = (S == 1) ? mixed_grid<1>(lay, np) : mixed_grid<2>(lay, np);
+    P.per_cta_a = lay.per_cta;
+    P.grid_b = 0;
+    P.smem_b = 0;
+  }
+  if (P.grid_a <= 0) return false;
+  size_t o = 256;  // work queues
+  P.off_blocks = o;
+  o += lay.blocks_d + lay.blocks_f;
+  P.off_ell = o;
+  o += lay.ell_bytes;
+  P.off_scratch = o;
+  o += (size_t)P.grid_a * P.per_cta_a;
+  P.off_lead = o;
+  if (P.warp_engine) o += al256((size_t)np * Bn * (8 + 8 + 16 * 4));
+  P.off_lstat = o;
+  if (P.warp_engine) o += al256((size_t)np * sizeof(int));
+  P.off_slabs = o;
+  if (P.warp_engine) o += al256((size_t)np * (L + 2) * Bn * (8 + 8 + 16));
+  P.total = o;
+  return true;
+}
+
+size_t mixed_workspace_bytes(int n, int nl, int nr, int L, int nq, int npts) {
+  MixedPlan P;
+  if (!make_plan(n, nl, nr, L, nq, npts, P)) return 0;
+  return P.total;
 }
 }  // namespace
 
@@ -385,7 +867,7 @@ int host_run(bool mixed, int refine_iters, int n, int nl, int nr, int L, int nq,
   const size_t b_Hld = (size_t)nq * nl * n * c16, b_Hrd = (size_t)nq * nr * n * c16;
   const size_t b_E = (size_t)npts * 8, b_i = (size_t)npts * 4;
   const size_t ws = mixed ? mixed_workspace_bytes(n, nl, nr, L, nq, npts)
-                          : workspace_bytes<double>(n, nl, nr, npts);
+                          : workspace_bytes<double>(n, nl, nr, nq, npts);
   if (ws == 0) return set_err(PF_ERR_SIZE, "pf: kernel does not fit on the device");
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t total = al(b_HL) * 2 + al(b_HR) * 2 + al(b_Hd) + al(b_Hdv) + al(b_Hld) + al(b_Hrd) + al(b_E) +
@@ -464,9 +946,9 @@ const char* pf_last_error(void) { return g_err; }
 
 int pf_version(void) { return PF_ABI_VERSION; }
 
-size_t pf_transport_tdb_workspace_size(int n, int nl, int nr, int npts) {
-  if (check_dims(n, nl, nr, 1, 1, npts) != PF_SUCCESS) return 0;
-  return workspace_bytes<double>(n, nl, nr, npts);
+size_t pf_transport_tdb_workspace_size(int n, int nl, int nr, int nq, int npts) {
+  if (check_dims(n, nl, nr, 1, nq, npts) != PF_SUCCESS) return 0;
+  return workspace_bytes<double>(n, nl, nr, nq, npts);
 }
 
 int pf_transport_tdb_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
@@ -484,7 +966,7 @@ int pf_transport_tdb_dev(int n, int nl, int nr, int L, int nq, const double* HL,
   if (max_iter <= 0) return set_err(PF_ERR_ARG, "pf: max_iter must be positive");
   pf::System<double> sys = make_sys(n, nl, nr, L, nq, HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd);
   pf::Points pts{npts, E, qidx, zero_flag};
-  pf::Params P{eta, eta0, dev_factor, convergence, max_iter, want_transr};
+  pf::Params P{nullptr, eta, eta0, dev_factor, convergence, max_iter, want_transr};
   pf::Outputs out{transl, want_transr ? transr : nullptr, status, iters};
   return launch_transport<double>(sys, pts, P, out, work, work_bytes, (cudaStream_t)stream);
 }
@@ -508,18 +990,18 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq, const doubl
   if (max_iter <= 0 || refine_iters < 0 || refine_iters > 16)
     return set_err(PF_ERR_ARG, "pf: max_iter must be positive and refine_iters in [0, 16]");
   if (npts == 0) return PF_SUCCESS;
-  MixedLayout lay = make_mixed_layout(n, nl, nr, L, nq);
+  MixedPlan plan;
+  if (!make_plan(n, nl, nr, L, nq, npts, plan)) return set_err(PF_ERR_SIZE, "pf: kernel does not fit on the device");
+  const MixedLayout& lay = plan.lay;
   DevInfo d = device_info();
   if (lay.smem > d.smem_optin) return set_err(PF_ERR_SIZE, "pf: working set exceeds shared memory");
   const int S = (lay.base.m + 31) / 32;
-  const int grid = (S == 1) ? mixed_grid<1>(lay, npts) : mixed_grid<2>(lay, npts);
-  if (grid <= 0) return set_err(PF_ERR_SIZE, "pf: kernel does not fit on the device");
-  const size_t need = 256 + lay.blocks_d + lay.blocks_f + (size_t)grid * lay.per_cta;
-  if (!work || work_bytes < need) return set_err(PF_ERR_ARG, "pf: workspace too small");
+  if (!work || work_bytes < plan.total) return set_err(PF_ERR_ARG, "pf: workspace too small");
   cudaStream_t st = (cudaStream_t)stream;
   char* w = reinterpret_cast<char*>(work);
   int* queue = reinterpret_cast<int*>(w);
-  char* p = w + 256;
+  int* queue_b = queue + 1;
+  char* p = w + plan.off_blocks;
   const double* src[8] = {HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd};
   dcx* dd[8];
   for (int i = 0; i < 8; ++i) {
@@ -531,7 +1013,20 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq, const doubl
     ff[i] = reinterpret_cast<fcx*>(p);
     p += (lay.cnt[i] * 8 + 255) & ~(size_t)255;
   }
-  char* scratch = p;
+  // ELL copies of the device-side blocks (residual of the refinement)
+  p = w + plan.off_ell;
+  int* ell_over = reinterpret_cast<int*>(p);
+  p += 256;
+  int* ecol[7];
+  dcx* eval[7];
+  for (int i = 0; i < 7; ++i) {
+    ecol[i] = reinterpret_cast<int*>(p);
+    p += (lay.ell_rows[i] * pf::PF_ELL_K * 4 + 255) & ~(size_t)255;
+    eval[i] = reinterpret_cast<dcx*>(p);
+    p += (lay.ell_rows[i] * pf::PF_ELL_K * 16 + 255) & ~(size_t)255;
+  }
+  int* mirror = reinterpret_cast<int*>(p);
+  char* scratch = w + plan.off_scratch;
   for (int i = 0; i < 8; ++i) {
     if (lay.cnt[i] == 0) continue;
     const int blocks = (int)((lay.cnt[i] + 255) / 256 < 4096 ? (lay.cnt[i] + 255) / 256 : 4096);
@@ -539,6 +1034,22 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq, const doubl
                                                    i >= 2 ? ff[i] : nullptr, lay.cnt[i]);
   }
   PF_CUDA(cudaGetLastError());
+  PF_CUDA(cudaMemsetAsync(ell_over, 0, sizeof(int), st));
+  {
+    struct F {
+      const dcx* m;
+      int rows, cols, count, ct;
+    } fam[7] = {{dd[4], n, n, nq * L, 0},           {dd[5], n, n, nq * (L - 1), 0}, {dd[5], n, n, nq * (L - 1), 1},
+                {dd[6], nl, n, nq, 0},              {dd[6], nl, n, nq, 1},          {dd[7], nr, n, nq, 0},
+                {dd[7], nr, n, nq, 1}};
+    for (int i = 0; i < 7; ++i) {
+      if (lay.ell_rows[i] == 0) continue;
+      const int blocks = (int)((lay.ell_rows[i] + 127) / 128 < 4096 ? (lay.ell_rows[i] + 127) / 128 : 4096);
+      build_ell_kernel<<<blocks, 128, 0, st>>>(fam[i].m, fam[i].rows, fam[i].cols, fam[i].count, fam[i].ct,
+                                                pf::PF_ELL_K, ecol[i], eval[i], ell_over);
+    }
+    PF_CUDA(cudaGetLastError());
+  }
   pf::MSys sys;
   sys.n = n;
   sys.nl = nl;
@@ -558,14 +1069,65 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq, const doubl
   sys.fHdv = ff[5];
   sys.fHld = ff[6];
   sys.fHrd = ff[7];
+  {
+    const int rows[7] = {n, n, n, nl, n, nr, n};
+    pf::Ell* es[7] = {&sys.eHd, &sys.eHdv, &sys.eHdvH, &sys.eHld, &sys.eHldH, &sys.eHrd, &sys.eHrdH};
+    for (int i = 0; i < 7; ++i) {
+      es[i]->col = ecol[i];
+      es[i]->val = eval[i];
+      es[i]->K = pf::PF_ELL_K;
+      es[i]->rows = rows[i];
+    }
+    sys.ell_overflow = ell_over;
+  }
   pf::Points pts{npts, E, qidx, zero_flag};
-  pf::Params P{eta, eta0, dev_factor, convergence, max_iter, 0};
+  pf::Params P{nullptr, eta, eta0, dev_factor, convergence, max_iter, 0};
+  if (nl == nr) {
+    lead_mirror_kernel<<<nq, 256, 0, st>>>(HL, HLv, HR, HRv, 2 * nl * nl, nq, mirror);
+    P.lead_mirror = mirror;
+  }
   pf::Outputs out{transl, nullptr, status, iters};
-  PF_CUDA(cudaMemsetAsync(queue, 0, sizeof(int), st));
-  if (S == 1)
-    mixed_kernel<1><<<grid, kThreads, lay.smem, st>>>(sys, pts, P, refine_iters, out, lay, scratch, queue);
-  else
-    mixed_kernel<2><<<grid, kThreads, lay.smem, st>>>(sys, pts, P, refine_iters, out, lay, scratch, queue);
+  PF_CUDA(cudaMemsetAsync(queue, 0, 2 * sizeof(int), st));
+  if (plan.warp_engine) {
+    const size_t Bn = (size_t)pf::wp::NW * pf::wp::NW;
+    const size_t np = (size_t)npts;
+    char* lp = w + plan.off_lead;
+    pf::wp::LeadOut lo;
+    lo.g0 = reinterpret_cast<fcx*>(lp);
+    lo.fsr = lo.g0 + np * Bn;
+    lo.esl = reinterpret_cast<dcx*>(lo.fsr + np * Bn);
+    lo.sr = lo.esl + np * Bn;
+    lo.gml = lo.sr + np * Bn;
+    lo.gmr = lo.gml + np * Bn;
+    int* lstat = reinterpret_cast<int*>(w + plan.off_lstat);
+    pf::wp::Slabs sl;
+    sl.lu = reinterpret_cast<fcx*>(w + plan.off_slabs);
+    sl.yv = sl.lu + np * (L + 2) * Bn;
+    sl.xv = reinterpret_cast<dcx*>(sl.yv + np * (L + 2) * Bn);
+    leads_kernel<1><<<plan.grid_a, kThreads, lay.smem, st>>>(sys, pts, P, out, lay, plan.per_cta_a, scratch, lo,
+                                                              lstat, queue);
+    PF_CUDA(cudaGetLastError());
+    // factorisation + back substitution, then each refinement sweep as a
+    // parallel residual kernel followed by the warp-per-point correction,
+    // then the Caroli trace
+    layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 0, out, lo, sl, lstat, queue_b);
+    PF_CUDA(cudaGetLastError());
+    const size_t rtotal = (size_t)npts * (L + 2) * Bn;
+    const int rblocks = (int)((rtotal + 255) / 256 < (size_t)d.sms * 16 ? (rtotal + 255) / 256 : (size_t)d.sms * 16);
+    for (int it = 0; it < refine_iters; ++it) {
+      residual_kernel<<<rblocks, 256, 0, st>>>(sys, pts, P, lo, sl);
+      PF_CUDA(cudaMemsetAsync(queue_b, 0, sizeof(int), st));
+      layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 1, out, lo, sl, lstat,
+                                                                         queue_b);
+      PF_CUDA(cudaGetLastError());
+    }
+    PF_CUDA(cudaMemsetAsync(queue_b, 0, sizeof(int), st));
+    layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 2, out, lo, sl, lstat, queue_b);
+  } else if (S == 1) {
+    mixed_kernel<1><<<plan.grid_a, kThreads, lay.smem, st>>>(sys, pts, P, refine_iters, out, lay, scratch, queue);
+  } else {
+    mixed_kernel<2><<<plan.grid_a, kThreads, lay.smem, st>>>(sys, pts, P, refine_iters, out, lay, scratch, queue);
+  }
   PF_CUDA(cudaGetLastError());
   return PF_SUCCESS;
 }

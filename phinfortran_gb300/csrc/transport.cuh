@@ -38,6 +38,7 @@ struct Points {
 };
 
 struct Params {
+  const int* lead_mirror;  // per q: 1 when HR == HL and HRv == HLv bitwise (may be null)
   double eta, eta0;     // lead broadening eps = E*eta + eta0
   double dev_factor;    // device broadening multiplier (10: phonon tdb, 1: tb)
   double convergence;   // decimation stop: maxval|alpha| <= convergence
@@ -165,7 +166,16 @@ __device__ int lead_pair(const Ctx<R>& c, const System<R>& sys, int q, double E,
     gamma_from_sigma(c.gs[G_GML], ld, c.sm[1], ld, nl, -1);  // -i(S - S^H) = -gml_adv
   }
   // right, retarded: z = E + i eps, alpha = Hamrv^H, beta = Hamrv
-  {
+  if (P.lead_mirror && P.lead_mirror[q]) {
+    // Identical leads: the right retarded decimation solves the adjoint of
+    // the left advanced problem (H00 hermitian, beta = alpha^H), so
+    // gr_ret = gl_adv^H, sr_ret = sl_adv^H, gmr_ret = -gml_adv -- exactly the
+    // wrapper-converted left quantities already in scratch.
+    copy_out(c.gs[G_GR], ld, false, c.gs[G_GL], ld, nl, nl);
+    copy_out(c.gs[G_SR], ld, false, c.gs[G_SL], ld, nl, nl);
+    copy_out(c.gs[G_GMR], ld, false, c.gs[G_GML], ld, nl, nl);
+    if (it_r) *it_r = *it_l;
+  } else {
     const cx<R>* HR = sys.HR + (size_t)q * nr * nr;
     const cx<R>* HRv = sys.HRv + (size_t)q * nr * nr;
     st |= decimate<R, S>(c, nr, mk<R>(R(E), R(eps)), opN<R>(HR, nr), opC<R>(HRv, nr),

@@ -153,7 +153,7 @@ class DeviceTransport:
         self.params = (eta, eta0, dev_factor, convergence, max_iter, int(bool(want_transr)))
         self.npts_max = npts_max
         if precision == "fp64":
-            ws = lib.pf_transport_tdb_workspace_size(n, nl, nr, npts_max)
+            ws = lib.pf_transport_tdb_workspace_size(n, nl, nr, nq, npts_max)
         else:
             ws = lib.pf_transport_tdb_mixed_workspace_size(n, nl, nr, L, nq, npts_max)
         if ws == 0:
