@@ -325,10 +325,12 @@ def main():
     else:
         torch.backends.cuda.matmul.allow_tf32 = False
         peak = measure_peak(torch, torch.complex64, 4096)
-        peak_src = ("cuBLAS CGEMM 4096^3 (FP32 SIMT, TF32 off) measured live on this GPU: the mixed kernel runs "
+        peak_src = ("cuBLAS CGEMM 4096^3 (FP32 SIMT, TF32 off) measured live on this GPU: the mixed pipeline runs "
                     "on the FP32 pipe (FP32 and double-float arithmetic); achieved counts the FP64-equivalent "
-                    "algorithmic flops F(n,L,I) only")
-        kernel = "mixed_kernel"
+                    "algorithmic flops F(n,L,I) per step only")
+        kernel = ("mixed pipeline per step: leads_kernel (double-float decimation, CTA per point) + layer_kernel "
+                  "(warp per point: FP32 LU, back substitution, refinement corrections, Caroli) + residual_kernel; "
+                  "achieved = F per step / step time")
     roof = dict(bound="tensor", achieved=achieved, peak=peak, unit="TFLOP/s", frac=achieved / peak, traffic=None,
                 peak_source=peak_src, kernel=kernel, algorithmic_flops_per_launch=fl,
                 flops_formula="n^3 (40 L + 16) + 2 n^3 (56 I + 24)", mean_decimation_iters=iters)
@@ -344,7 +346,12 @@ def main():
         v, cores, sample = cpu_oracle_rate(E, b, p)
         cpu = dict(value=v, unit="solves/s", cores=cores, kind="port", sample=sample)
 
-    launches_per_step = 1 if args.path == "fp64" else 9   # mixed: 8 block conversions + 1 transport kernel
+    if args.path == "fp64":
+        launches_per_step = 2                         # lead-mirror check + transport_kernel
+    else:
+        # 8 block conversions + 7 ELL builds + lead-mirror check + leads_kernel + layer_kernel (factor)
+        # + per refinement (residual_kernel + layer_kernel) + point-energy kernel + layer_kernel (Caroli)
+        launches_per_step = 8 + 7 + 1 + 1 + 1 + 2 * args.refine + (1 if args.refine else 0) + 1
     line = dict(metric=METRIC, value=value, unit="solves/s", n_gpus=ws, steps=args.steps, warmup=args.warmup,
                 ms_per_step=t_step * 1e3, higher_is_better=True, scaling="weak", vs_baseline=None,
                 dtype="complex128 (fp64)" if args.path == "fp64" else "complex: fp32 + double-float (no fp64 ops)",

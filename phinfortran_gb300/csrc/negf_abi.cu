@@ -523,7 +523,17 @@ __device__ __forceinline__ dcx dense_acc(const dcx* M, int ldm, int kdim, bool c
   return acc;
 }
 
-__global__ void residual_kernel(pf::MSys s, pf::Points pts, pf::Params P, pf::wp::LeadOut lo, pf::wp::Slabs sl) {
+// Per-point energies in df64: zL = E + i eps, zD = E + i dev_factor eps.
+__global__ void point_z_kernel(pf::Points pts, pf::Params P, dcx* z2) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= pts.npts) return;
+  const double E = pts.E[p];
+  const double eps = E * P.eta + P.eta0;
+  z2[2 * p] = pf::mk<pf::df64>(pf::df64(E), pf::df64(eps));
+  z2[2 * p + 1] = pf::mk<pf::df64>(pf::df64(E), pf::df64(P.dev_factor * eps));
+}
+
+__global__ void residual_kernel(pf::MSys s, pf::Points pts, const dcx* z2, pf::wp::LeadOut lo, pf::wp::Slabs sl) {
   const int NW = pf::wp::NW;
   const size_t B = (size_t)NW * NW;
   const int L = s.L, n = s.n;
@@ -540,9 +550,7 @@ __global__ void residual_kernel(pf::MSys s, pf::Points pts, pf::Params P, pf::wp
     fcx outv = pf::mk<float>(0.f, 0.f);
     if (r < dj && c < s.nr) {
       const int q = pts.qidx ? pts.qidx[p] : 0;
-      const double E = pts.E[p];
-      const double eps = E * P.eta + P.eta0;
-      const dcx z = pf::mk<pf::df64>(pf::df64(E), pf::df64((j == 0 ? 1.0 : P.dev_factor) * eps));
+      const dcx z = z2[2 * p + (j == 0 ? 0 : 1)];
       const dcx* xb = sl.xv + (size_t)p * per_pt;
       const dcx* X0 = xb + (size_t)j * B;
       dcx acc = pf::csub(pf::wp::dz(), pf::cmul(z, X0[r + c * NW]));
@@ -767,7 +775,7 @@ struct MixedPlan {
   bool warp_engine;     // cross-sections <= 32: leads kernel + warp-per-point layer kernel
   int grid_a, grid_b;   // CTA counts of the (leads / fused) kernel and the layer kernel
   size_t per_cta_a;     // per-CTA scratch of kernel A
-  size_t off_blocks, off_ell, off_scratch, off_lead, off_lstat, off_slabs, total;
+  size_t off_blocks, off_ell, off_scratch, off_lead, off_lstat, off_z, off_slabs, total;
   size_t smem_b;
 };
 
@@ -827,6 +835,8 @@ bool make_plan(int n, int nl, int nr, int L, int nq, int npts, MixedPlan& P) {
   if (P.warp_engine) o += al256((size_t)np * Bn * (8 + 8 + 16 * 4));
   P.off_lstat = o;
   if (P.warp_engine) o += al256((size_t)np * sizeof(int));
+  P.off_z = o;
+  if (P.warp_engine) o += al256((size_t)np * 2 * 16);
   P.off_slabs = o;
   if (P.warp_engine) o += al256((size_t)np * (L + 2) * Bn * (8 + 8 + 16));
   P.total = o;
@@ -1114,8 +1124,10 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq, const doubl
     PF_CUDA(cudaGetLastError());
     const size_t rtotal = (size_t)npts * (L + 2) * Bn;
     const int rblocks = (int)((rtotal + 255) / 256 < (size_t)d.sms * 16 ? (rtotal + 255) / 256 : (size_t)d.sms * 16);
+    dcx* z2 = reinterpret_cast<dcx*>(w + plan.off_z);
+    if (refine_iters > 0) point_z_kernel<<<(npts + 127) / 128, 128, 0, st>>>(pts, P, z2);
     for (int it = 0; it < refine_iters; ++it) {
-      residual_kernel<<<rblocks, 256, 0, st>>>(sys, pts, P, lo, sl);
+      residual_kernel<<<rblocks, 256, 0, st>>>(sys, pts, z2, lo, sl);
       PF_CUDA(cudaMemsetAsync(queue_b, 0, sizeof(int), st));
       layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 1, out, lo, sl, lstat,
                                                                          queue_b);

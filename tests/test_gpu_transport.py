@@ -101,8 +101,9 @@ def test_tb_ribbon_full_size_properties(cuda_ready):
     # where the oracle is integral.
     b0, E0, p0 = S.tb_ribbon(disorder=0.0, L=50, ne=200, eta=1e-10)
     r0 = transport_tdb(E0, b0, want_transr=False, **p0)
-    o0 = N.transport(E0, b0, p0["eta"], p0["eta0"], p0["convergence"], p0["dev_factor"])
-    assert np.abs(r0["transl"] - o0["transl"]).max() < 1e-6
+    o0, floor0 = fp64_noise_floor(E0, b0, p0)
+    # near degenerate subband crossings FP64 itself is reproducible only to ~1e-4
+    assert (np.abs(r0["transl"] - o0["transl"]) <= np.maximum(1e-10, 20 * floor0)).all()
     integral = np.abs(o0["transl"] - np.round(o0["transl"])) < 1e-8
     assert integral.mean() > 0.8
     assert np.abs(r0["transl"][integral] - np.round(r0["transl"][integral])).max() < 1e-7
