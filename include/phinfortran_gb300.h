@@ -158,6 +158,37 @@ int pf_transport_tdb_mixed(int n, int nl, int nr, int L, int nq,
                            double convergence, int max_iter, int refine_iters,
                            double* transl, int* status, int* iters);
 
+/*
+ * Allocation-free variant of pf_transport_tdb_dev.  No counterpart in the
+ * reference (whose Fortran arrays are all allocated by the driver): it
+ * serves callers that cannot give this library a device workspace -- host
+ * codes that reserve the GPU's memory up front through their own allocator
+ * and forbid any later cudaMalloc.  It takes the same device arrays as
+ * pf_transport_tdb_dev minus `work`/`work_bytes` and calls no cudaMalloc,
+ * cudaFree or allocating library routine.  Its scratch is a static device
+ * array of PF_NOALLOC_SCRATCH_BYTES that every GPU loading the library
+ * holds until the process exits; problems whose minimum scratch exceeds it
+ * are rejected with PF_ERR_SIZE, and large batches run with fewer
+ * concurrent CTAs.  The first call on a device resolves the array's device
+ * address (cudaGetSymbolAddress, with that device current); make that first
+ * call before any stream capture.  All calls share the array: calls whose
+ * kernels overlap on the GPU (concurrent streams, several host threads)
+ * race on it and must be serialised by the caller.
+ */
+#define PF_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+int pf_transport_tdb_noalloc(int n, int nl, int nr, int L, int nq,
+                             const double* HL, const double* HLv,
+                             const double* HR, const double* HRv,
+                             const double* Hd, const double* Hdv,
+                             const double* Hld, const double* Hrd,
+                             int npts, const double* E, const int* qidx,
+                             const int* zero_flag,
+                             double eta, double eta0, double dev_factor,
+                             double convergence, int max_iter, int want_transr,
+                             double* transl, double* transr, int* status,
+                             int* iters, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

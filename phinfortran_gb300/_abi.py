@@ -42,6 +42,14 @@ SIGNATURES = {
                                          C.c_double, C.c_double, C.c_double, C.c_double,
                                          C.c_int, C.c_int,
                                          _dp, _ip, _ip]),
+    "pf_transport_tdb_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_double, C.c_double, C.c_double, C.c_double,
+                                           C.c_int, C.c_int,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p]),
     "pf_transport_tdb": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                    _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                    C.c_int, _dp, _ip, _ip,

@@ -848,6 +848,88 @@ size_t mixed_workspace_bytes(int n, int nl, int nr, int L, int nq, int npts) {
   if (!make_plan(n, nl, nr, L, nq, npts, P)) return 0;
   return P.total;
 }
+
+// ===========================================================================
+// Allocation-free variant of the FP64 transport entry.
+//
+// Some callers cannot hand this library a device workspace: host codes that
+// reserve the GPU's memory up front through their own allocator and forbid
+// any later cudaMalloc (or cannot expose a device pointer for scratch at
+// the call site).  For them pf_transport_tdb_noalloc keeps its scratch --
+// the work-queue counter, the lead-mirror flags and the per-CTA matrices of
+// the persistent kernel -- in the file-scope array below.  Every GPU that
+// loads the library holds PF_NOALLOC_SCRATCH_BYTES of it until the process
+// exits.  All calls share the array and it keeps the contents of the last
+// call: the queue counter is cleared and the mirror flags rewritten on
+// every call, and calls whose kernels overlap on the GPU race on it.
+// ===========================================================================
+static __device__ __align__(256) unsigned char g_noalloc_scratch[PF_NOALLOC_SCRATCH_BYTES];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[128] = {};
+
+// Device address of the static scratch for the current device; resolved
+// once per device (the first call on a device does it, with that device
+// current).
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  PF_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return set_err(PF_ERR_ARG, "pf: device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_err(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_ptr[dev];
+  return PF_SUCCESS;
+}
+
+// Same launch as launch_transport, with the persistent grid capped so that
+// the per-CTA scratch fits in the static array.
+int launch_transport_noalloc(const pf::System<double>& sys, const pf::Points& pts, const pf::Params& P,
+                             const pf::Outputs& out, cudaStream_t stream) {
+  const Layout lay = make_layout<double>(sys.n, sys.nl, sys.nr);
+  DevInfo d = device_info();
+  if (lay.smem > d.smem_optin) return set_err(PF_ERR_SIZE, "pf: working set exceeds shared memory");
+  const size_t mir = ((size_t)sys.nq * sizeof(int) + 255) & ~(size_t)255;
+  const size_t fixed = 256 + mir;
+  if (fixed + lay.per_cta_bytes > (size_t)PF_NOALLOC_SCRATCH_BYTES)
+    return set_err(PF_ERR_SIZE,
+                   "pf_transport_tdb_noalloc: problem needs more scratch than the static maximum "
+                   "PF_NOALLOC_SCRATCH_BYTES (too many q points or too large blocks)");
+  if (pts.npts == 0) return PF_SUCCESS;
+  const int S = (lay.m + 31) / 32;
+  int grid = (S == 1) ? grid_for<double, 1>(lay, pts.npts) : grid_for<double, 2>(lay, pts.npts);
+  if (grid <= 0) return set_err(PF_ERR_SIZE, "pf: kernel does not fit on the device");
+  const size_t cap = ((size_t)PF_NOALLOC_SCRATCH_BYTES - fixed) / lay.per_cta_bytes;
+  if ((size_t)grid > cap) grid = (int)cap;
+  void* base = nullptr;
+  int rc = noalloc_scratch(&base);
+  if (rc != PF_SUCCESS) return rc;
+  int* queue = reinterpret_cast<int*>(base);
+  int* mirror = reinterpret_cast<int*>(reinterpret_cast<char*>(base) + 256);
+  char* gscr = reinterpret_cast<char*>(base) + fixed;
+  PF_CUDA(cudaMemsetAsync(queue, 0, sizeof(int), stream));
+  pf::Params P2 = P;
+  if (sys.nl == sys.nr) {
+    lead_mirror_kernel<<<sys.nq, 256, 0, stream>>>(reinterpret_cast<const double*>(sys.HL),
+                                                   reinterpret_cast<const double*>(sys.HLv),
+                                                   reinterpret_cast<const double*>(sys.HR),
+                                                   reinterpret_cast<const double*>(sys.HRv), 2 * sys.nl * sys.nl,
+                                                   sys.nq, mirror);
+    P2.lead_mirror = mirror;
+  } else {
+    P2.lead_mirror = nullptr;
+  }
+  if (S == 1)
+    transport_kernel<double, 1><<<grid, kThreads, lay.smem, stream>>>(sys, pts, P2, out, lay, gscr, queue);
+  else
+    transport_kernel<double, 2><<<grid, kThreads, lay.smem, stream>>>(sys, pts, P2, out, lay, gscr, queue);
+  PF_CUDA(cudaGetLastError());
+  return PF_SUCCESS;
+}
 }  // namespace
 
 extern "C" int pf_transport_tdb_dev(int, int, int, int, int, const double*, const double*, const double*,
@@ -1160,6 +1242,26 @@ int pf_transport_tdb(int n, int nl, int nr, int L, int nq, const double* HL, con
                      int want_transr, double* transl, double* transr, int* status, int* iters) {
   return host_run(false, 0, n, nl, nr, L, nq, HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd, npts, E, qidx, zero_flag, eta,
                   eta0, dev_factor, convergence, max_iter, want_transr, transl, transr, status, iters);
+}
+
+int pf_transport_tdb_noalloc(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
+                             const double* HR, const double* HRv, const double* Hd, const double* Hdv,
+                             const double* Hld, const double* Hrd, int npts, const double* E, const int* qidx,
+                             const int* zero_flag, double eta, double eta0, double dev_factor, double convergence,
+                             int max_iter, int want_transr, double* transl, double* transr, int* status,
+                             int* iters, void* stream) {
+  int rc = check_dims(n, nl, nr, L, nq, npts);
+  if (rc != PF_SUCCESS) return rc;
+  if (!E || !transl || !status || (want_transr && !transr))
+    return set_err(PF_ERR_ARG, "pf: null energy/output pointer");
+  if (!HL || !HLv || !HR || !HRv || !Hd || !Hld || !Hrd || (L > 1 && !Hdv))
+    return set_err(PF_ERR_ARG, "pf: null block pointer");
+  if (max_iter <= 0) return set_err(PF_ERR_ARG, "pf: max_iter must be positive");
+  pf::System<double> sys = make_sys(n, nl, nr, L, nq, HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd);
+  pf::Points pts{npts, E, qidx, zero_flag};
+  pf::Params P{nullptr, eta, eta0, dev_factor, convergence, max_iter, want_transr};
+  pf::Outputs out{transl, want_transr ? transr : nullptr, status, iters};
+  return launch_transport_noalloc(sys, pts, P, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"
