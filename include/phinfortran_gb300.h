@@ -159,6 +159,52 @@ int pf_transport_tdb_mixed(int n, int nl, int nr, int L, int nq,
                            double* transl, int* status, int* iters);
 
 /*
+ * Block dynamical matrices of the tdb branch for nq transverse q points,
+ * assembled on the GPU.  Replaces gen_dyn_qe_tdb_k (negf/dyn.f90:1482-2080),
+ * called by gen_dyn_qe_tdb_mpi once per k (negf/phinfortran.f90:1189).
+ * Inputs are the reference's own arrays, Fortran layout:
+ *   fc(3,3,nat,nat,nx,ny,nz) (THz^2 amu, after cutoff and ASR, fc.f90:204-266),
+ *   cell(3,3) (QE cell, row i = vector i), cell_all(3,3) (supercell),
+ *   pos(nat,3), pos_all(natall,3), idxall(natall) (1-based basis index),
+ *   mass_all(natall), rws(124,3), rd(124) (fc.f90:271-289),
+ *   kgrid(nq,3) fractional (config.f90:153-188 after k_grid_in_ws).
+ * Outputs (host arrays, interleaved complex, the layout pf_transport_tdb
+ * takes): HL,HLv [nq][3pl x 3pl], HR,HRv [nq][3pr x 3pr],
+ * Hd [nq][nlayer][3na x 3na], Hdv [nq][nlayer-1][3na x 3na],
+ * Hld [nq][3pl x 3na], Hrd [nq][3pr x 3na]  (pl = period_left,
+ * pr = period_right, na = natm_layer).  Like the reference, the blocks are
+ * not hermitised.
+ */
+int pf_gen_dyn_qe_tdb(int nat, int nx, int ny, int nz, const double* fc,
+                      const double* cell, const double* cell_all,
+                      const double* pos, int natall, const double* pos_all,
+                      const int* idxall, const double* mass_all,
+                      const double* rws, const double* rd,
+                      int n_bloch_x, int n_bloch_y,
+                      int buffer_left, int period_left,
+                      int buffer_right, int period_right,
+                      int nlayer, int natm_layer,
+                      int nq, const double* kgrid,
+                      double* HL, double* HLv, double* HR, double* HRv,
+                      double* Hd, double* Hdv, double* Hld, double* Hrd);
+
+/* Message for the last error of pf_gen_dyn_qe_tdb on the calling thread. */
+const char* pf_dyn_last_error(void);
+
+/*
+ * Two-probe Landauer conductance for ntemp temperatures (host arrays):
+ * sigma[t] = 1/area * 1/(2 pi) * trapz(hbar w df/dT trans(w), w), the
+ * formula of examples/negf/si-si/condt.py:14-30 (omega in rad/s, SI units,
+ * trans already averaged over k as condt.py:44-51 does).
+ */
+int pf_landauer_conductance(int ne, const double* omega, const double* trans,
+                            int ntemp, const double* temps, double area,
+                            double* sigma);
+
+/* Message for the last error of pf_landauer_conductance. */
+const char* pf_cond_last_error(void);
+
+/*
  * Allocation-free variant of pf_transport_tdb_dev.  No counterpart in the
  * reference (whose Fortran arrays are all allocated by the driver): it
  * serves callers that cannot give this library a device workspace -- host

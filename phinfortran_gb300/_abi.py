@@ -50,6 +50,13 @@ SIGNATURES = {
                                            C.c_int, C.c_int,
                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.c_void_p]),
+    "pf_dyn_last_error": (C.c_char_p, []),
+    "pf_gen_dyn_qe_tdb": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp,
+                                    _dp, C.c_int, _dp, _ip, _dp, _dp, _dp, C.c_int, C.c_int,
+                                    C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "pf_cond_last_error": (C.c_char_p, []),
+    "pf_landauer_conductance": (C.c_int, [C.c_int, _dp, _dp, C.c_int, _dp, C.c_double, _dp]),
     "pf_transport_tdb": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                    _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                    C.c_int, _dp, _ip, _ip,
