@@ -205,6 +205,40 @@ int pf_landauer_conductance(int ne, const double* omega, const double* trans,
 const char* pf_cond_last_error(void);
 
 /*
+ * Adjoint of the transmission (FP64), device pointers.  No counterpart in
+ * the reference (the derivative that an inverse design or a thermal-
+ * conductance optimisation needs).  For the points of a batch with weights
+ * w_p (NULL: all 1; points with zero_flag get weight 0) it returns T_L of
+ * every point (as pf_transport_tdb_dev) and accumulates
+ *     M_B = sum_p w_p dT_p/dB,   dF = Re Tr[dB M_B],  F = sum_p w_p T_p,
+ * for the device blocks and the lead-device couplings:
+ *   gHd [nq][L][n x n], gHdv [nq][L-1][n x n], gHld [nq][n x nl],
+ *   gHrd [nq][n x nr]  (device arrays, interleaved complex, zeroed here).
+ * The lead cells (HL, HLv, HR, HRv) are held fixed.  The cost is about
+ * 2.6x one forward sweep (block LU, two block-column solves, contractions).
+ * work must hold pf_transport_tdb_grad_workspace_size(...) bytes.
+ */
+size_t pf_transport_tdb_grad_workspace_size(int n, int nl, int nr, int L,
+                                            int nq, int npts);
+
+int pf_transport_tdb_grad_dev(int n, int nl, int nr, int L, int nq,
+                              const double* HL, const double* HLv,
+                              const double* HR, const double* HRv,
+                              const double* Hd, const double* Hdv,
+                              const double* Hld, const double* Hrd,
+                              int npts, const double* E, const int* qidx,
+                              const int* zero_flag, const double* weights,
+                              double eta, double eta0, double dev_factor,
+                              double convergence, int max_iter,
+                              double* transl, int* status, int* iters,
+                              double* gHd, double* gHdv, double* gHld,
+                              double* gHrd, void* work, size_t work_bytes,
+                              void* stream);
+
+/* Message for the last error of the gradient entry points. */
+const char* pf_grad_last_error(void);
+
+/*
  * Allocation-free variant of pf_transport_tdb_dev.  No counterpart in the
  * reference (whose Fortran arrays are all allocated by the driver): it
  * serves callers that cannot give this library a device workspace -- host

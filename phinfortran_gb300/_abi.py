@@ -57,6 +57,16 @@ SIGNATURES = {
                                     C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "pf_cond_last_error": (C.c_char_p, []),
     "pf_landauer_conductance": (C.c_int, [C.c_int, _dp, _dp, C.c_int, _dp, C.c_double, _dp]),
+    "pf_grad_last_error": (C.c_char_p, []),
+    "pf_transport_tdb_grad_workspace_size": (C.c_size_t, [C.c_int] * 6),
+    "pf_transport_tdb_grad_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                            C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_size_t, C.c_void_p]),
     "pf_transport_tdb": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                    _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                    C.c_int, _dp, _ip, _ip,
