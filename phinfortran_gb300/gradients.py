@@ -26,50 +26,79 @@ THZ2RADS = 1e12 * np.pi * 2
 
 def _unpack(buf, shape):
     """Column-major interleaved complex device buffer -> numpy (.., rows, cols)."""
-    z = buf.cpu().numpy().view(np.complex128)
+    z = buf.cpu().numpy().view(np.complex128)[:int(np.prod(shape))]
     *lead, r, c = shape
     return z.reshape(tuple(lead) + (c, r)).swapaxes(-1, -2)
+
+
+class DeviceGradient:
+    """Blocks, accumulators and scratch resident in HBM for repeated adjoint
+    launches; ``run`` takes device-resident energies and weights."""
+
+    def __init__(self, blocks, npts_max, *, eta, eta0, convergence, dev_factor=10.0, max_iter=1000,
+                 device="cuda"):
+        import torch
+        self.torch = torch
+        lib = _abi.load()
+        if isinstance(blocks, dict):
+            blocks = TdbBlocks.from_dict(blocks)
+        nq, (n, nl, nr, L), arrs = blocks.stacked()
+        self.dims = (n, nl, nr, L, nq)
+        self.dev = {k: torch.from_numpy(fortran_block(v).copy()).to(device) for k, v in arrs.items()}
+        self.params = (eta, eta0, dev_factor, convergence, max_iter)
+        self.npts_max = npts_max
+        self.shapes = dict(Hd=(nq, L, n, n), Hdv=(nq, max(L - 1, 0), n, n), Hld=(nq, n, nl), Hrd=(nq, n, nr))
+        self.g = {k: torch.zeros(max(2 * int(np.prod(s)), 2), dtype=torch.float64, device=device)
+                  for k, s in self.shapes.items()}
+        ws = lib.pf_transport_tdb_grad_workspace_size(n, nl, nr, L, nq, npts_max)
+        if ws == 0:
+            raise _abi.PFError(-3, "gradient kernel does not fit (block size > 48?)")
+        self.work = torch.empty(ws, dtype=torch.uint8, device=device)
+        self.transl = torch.zeros(npts_max, dtype=torch.float64, device=device)
+        self.status = torch.zeros(npts_max, dtype=torch.int32, device=device)
+        self.iters = torch.zeros((npts_max, 2), dtype=torch.int32, device=device)
+
+    def run(self, E, weights=None, qidx=None, zero_flag=None, stream=None):
+        torch = self.torch
+        lib = _abi.load()
+        n, nl, nr, L, nq = self.dims
+        npts = int(E.shape[0])
+        if npts > self.npts_max:
+            raise ValueError("more points than allocated")
+        s = stream if stream is not None else torch.cuda.current_stream()
+        eta, eta0, dev_factor, conv, max_iter = self.params
+        p = lambda t: None if t is None else t.data_ptr()
+        g = self.g
+        rc = lib.pf_transport_tdb_grad_dev(n, nl, nr, L, nq, *[self.dev[k].data_ptr() for k in BLOCK_NAMES],
+                                           npts, E.data_ptr(), p(qidx), p(zero_flag), p(weights), eta, eta0,
+                                           dev_factor, conv, max_iter, self.transl.data_ptr(),
+                                           self.status.data_ptr(), self.iters.data_ptr(), g["Hd"].data_ptr(),
+                                           g["Hdv"].data_ptr() if L > 1 else None, g["Hld"].data_ptr(),
+                                           g["Hrd"].data_ptr(), self.work.data_ptr(), self.work.numel(),
+                                           C.c_void_p(s.cuda_stream))
+        if rc != 0:
+            raise _abi.PFError(rc, lib.pf_grad_last_error().decode(errors="replace"))
+        return self.transl[:npts], self.status[:npts]
+
+    def sensitivities(self):
+        """M dict (leading q axis) as numpy, after the stream has finished."""
+        return {k: _unpack(self.g[k], s) for k, s in self.shapes.items()}
 
 
 def transport_grad(E, blocks, weights=None, *, eta, eta0, convergence, dev_factor=10.0, qidx=None,
                    zero_flag=None, max_iter=1000, check=True):
     """Forward T (npts,) and M dict (leading q axis) through the adjoint kernel."""
     import torch
-    lib = _abi.load()
-    if isinstance(blocks, dict):
-        blocks = TdbBlocks.from_dict(blocks)
-    nq, (n, nl, nr, L), arrs = blocks.stacked()
-    dev = {k: torch.from_numpy(fortran_block(v).copy()).cuda() for k, v in arrs.items()}
     E = np.ascontiguousarray(E, dtype=np.float64)
-    npts = E.size
-    Ed = torch.from_numpy(E).cuda()
-    wd = None if weights is None else torch.from_numpy(np.ascontiguousarray(weights, dtype=np.float64)).cuda()
-    qd = None if qidx is None else torch.from_numpy(np.ascontiguousarray(qidx, dtype=np.int32)).cuda()
-    zd = None if zero_flag is None else torch.from_numpy(np.ascontiguousarray(zero_flag, dtype=np.int32)).cuda()
-    tl = torch.zeros(npts, dtype=torch.float64, device="cuda")
-    st = torch.zeros(npts, dtype=torch.int32, device="cuda")
-    it = torch.zeros(2 * npts, dtype=torch.int32, device="cuda")
-    shapes = dict(Hd=(nq, L, n, n), Hdv=(nq, max(L - 1, 0), n, n), Hld=(nq, n, nl), Hrd=(nq, n, nr))
-    g = {k: torch.zeros(2 * int(np.prod(s)), dtype=torch.float64, device="cuda") for k, s in shapes.items()}
-    ws = lib.pf_transport_tdb_grad_workspace_size(n, nl, nr, L, nq, npts)
-    if ws == 0:
-        raise _abi.PFError(-3, "gradient kernel does not fit (block size > 48?)")
-    work = torch.empty(ws, dtype=torch.uint8, device="cuda")
-    p = lambda t: None if t is None else t.data_ptr()
-    rc = lib.pf_transport_tdb_grad_dev(n, nl, nr, L, nq, *[dev[k].data_ptr() for k in BLOCK_NAMES], npts,
-                                       Ed.data_ptr(), p(qd), p(zd), p(wd), eta, eta0, dev_factor, convergence,
-                                       max_iter, tl.data_ptr(), st.data_ptr(), it.data_ptr(),
-                                       g["Hd"].data_ptr(), g["Hdv"].data_ptr() if L > 1 else None,
-                                       g["Hld"].data_ptr(), g["Hrd"].data_ptr(), work.data_ptr(), ws,
-                                       C.c_void_p(torch.cuda.current_stream().cuda_stream))
-    if rc != 0:
-        raise _abi.PFError(rc, lib.pf_grad_last_error().decode(errors="replace"))
+    dg = DeviceGradient(blocks, max(E.size, 1), eta=eta, eta0=eta0, convergence=convergence,
+                        dev_factor=dev_factor, max_iter=max_iter)
+    dev = lambda a, dt: None if a is None else torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).cuda()
+    tl, st = dg.run(dev(E, np.float64), dev(weights, np.float64), dev(qidx, np.int32), dev(zero_flag, np.int32))
     torch.cuda.synchronize()
     status = st.cpu().numpy()
     if check and (status != 0).any():
         raise _abi.PFError(-4, f"point status flags 0x{int(np.bitwise_or.reduce(status)):x}")
-    M = {k: _unpack(g[k], s) for k, s in shapes.items()}
-    return tl.cpu().numpy(), M, status
+    return tl.cpu().numpy(), dg.sensitivities(), status
 
 
 def landauer_weights(omega_thz, temperature, area=1.0):
