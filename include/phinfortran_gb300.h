@@ -269,6 +269,53 @@ int pf_transport_tdb_noalloc(int n, int nl, int nr, int L, int nq,
                              double* transl, double* transr, int* status,
                              int* iters, void* stream);
 
+/*
+ * Mode-resolved transmission (replaces vel_mat_tdb_mpi,
+ * negf/velocity_mat.f90:227-279, with vel_mat_tdb at
+ * negf/velocity_mat.f90:1692-3148, called per (ie, ik) from
+ * negf/phinfortran.f90:1238-1250 together with the surface and RGF calls
+ * that feed it).  FP64.  For each point it runs the four lead
+ * decimations, both sweeps and the Caroli traces (transl/transr as
+ * pf_transport_tdb_dev with want_transr = 1), then the Bloch eigenmodes of
+ * the four transfer matrices, the velocity matrices, the t/r matrices and
+ * their specular / non-specular sums, written to mode_sums[8*p + k] in the
+ * order transl_s, transl_ns, transr_s, transr_ns, refll_s, refll_ns,
+ * reflr_s, reflr_ns (the reduce arrays of the reference's driver).
+ *   lambda_eta        : propagating test | |lambda| - 1 | < lambda_eta
+ *   a_z_l, a_z_r      : lead periods along transport (a_z_L, a_z_R)
+ *   nshift            : folded k shifts (n_bloch_x * n_bloch_y)
+ *   stride_*, nrep_*  : orbital stride between transverse images of the
+ *                       lead layer and the orbitals of one image
+ *   phase_l, phase_r  : unfolding phases [nq][nshift][nl|nr] complex,
+ *                       exp(-i(-p.k_sc + (p - p_uc).k_shift)) per orbital
+ *                       (velocity_mat.f90:2035-2072); built by the caller
+ *   nprop             : optional [npts][4] propagating-mode counts of the
+ *                       adv-L, ret-L, ret-R, adv-R problems
+ * Points flagged in zero_flag get zero t/r sums (the ie == 1 rule).
+ * Status bit 8: a Schur (QR) iteration did not converge.
+ */
+size_t pf_transport_tdb_modes_workspace_size(int n, int nl, int nr, int nq, int npts);
+
+int pf_transport_tdb_modes_dev(int n, int nl, int nr, int L, int nq,
+                               const double* HL, const double* HLv,
+                               const double* HR, const double* HRv,
+                               const double* Hd, const double* Hdv,
+                               const double* Hld, const double* Hrd,
+                               int npts, const double* E, const int* qidx,
+                               const int* zero_flag,
+                               double eta, double eta0, double dev_factor,
+                               double convergence, int max_iter,
+                               double lambda_eta, double a_z_l, double a_z_r,
+                               int nshift, int stride_l, int nrep_l,
+                               const double* phase_l, int stride_r, int nrep_r,
+                               const double* phase_r,
+                               double* transl, double* transr,
+                               double* mode_sums, int* status, int* nprop,
+                               void* work, size_t work_bytes, void* stream);
+
+/* Message for the last error of the mode-resolved entry point. */
+const char* pf_modes_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

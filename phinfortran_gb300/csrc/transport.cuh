@@ -193,7 +193,8 @@ __device__ int lead_pair(const Ctx<R>& c, const System<R>& sys, int q, double E,
 // Slots: SM0 = V, SM1 = T, SM2 = A (inverted), SM3 = g; G_W2 = G0N, G_W3 = U.
 // ----------------------------------------------------------------------------
 template <typename R, int S>
-__device__ int sweep_lr(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, double* trans) {
+__device__ int sweep_lr(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, double* trans,
+                        cx<R>* out_glr = nullptr, cx<R>* out_gr = nullptr, int ldo = 0) {
   const int ld = c.ld;
   const int n = sys.n, nl = sys.nl, nr = sys.nr, L = sys.L;
   cx<R>* V = c.sm[0];
@@ -237,7 +238,10 @@ __device__ int sweep_lr(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, 
   st |= inverse(A, ld, nr, c.iw);
   row_gemm<R, S>(nl, nr, n, opN<R>(G0N, ld), opC<R>(V, ld), EpiStore<R>{U, ld, mk<R>(1, 0)});
   row_gemm<R, S>(nl, nr, nr, opN<R>(U, ld), opN<R>(A, ld), EpiStore<R>{T, ld, mk<R>(1, 0)});
-  // T now holds G_D_LR = G_{0,N+1} (nl x nr).  Caroli: Re Tr[(G gmr)(G^H gml)]
+  // T now holds G_D_LR = G_{0,N+1} (nl x nr), A holds G_R = G_{N+1,N+1}
+  if (out_glr) copy_out(out_glr, ldo, false, T, ld, nl, nr);
+  if (out_gr) copy_out(out_gr, ldo, false, A, ld, nr, nr);
+  // Caroli: Re Tr[(G gmr)(G^H gml)]
   copy_in(A, ld, opN<R>(c.gs[G_GMR], ld), nr, nr);
   row_gemm<R, S>(nl, nr, nr, opN<R>(T, ld), opN<R>(A, ld), EpiStore<R>{U, ld, mk<R>(1, 0)});
   copy_in(A, ld, opN<R>(c.gs[G_GML], ld), nl, nl);
@@ -250,7 +254,8 @@ __device__ int sweep_lr(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, 
 // Right-to-left sweep + Caroli T_R (lesser.f90:694-793).
 // ----------------------------------------------------------------------------
 template <typename R, int S>
-__device__ int sweep_rl(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, double* trans) {
+__device__ int sweep_rl(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, double* trans,
+                        cx<R>* out_grl = nullptr, cx<R>* out_gl = nullptr, int ldo = 0) {
   const int ld = c.ld;
   const int n = sys.n, nl = sys.nl, nr = sys.nr, L = sys.L;
   cx<R>* V = c.sm[0];
@@ -295,7 +300,10 @@ __device__ int sweep_rl(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, 
   st |= inverse(A, ld, nl, c.iw);
   row_gemm<R, S>(nr, nl, n, opN<R>(GNo, ld), opC<R>(V, ld), EpiStore<R>{U, ld, mk<R>(1, 0)});
   row_gemm<R, S>(nr, nl, nl, opN<R>(U, ld), opN<R>(A, ld), EpiStore<R>{T, ld, mk<R>(1, 0)});
-  // T = G_D_RL (nr x nl).  Caroli: Re Tr[(G gml)(G^H gmr)]
+  // T = G_D_RL (nr x nl), A = G_L = G_{0,0}
+  if (out_grl) copy_out(out_grl, ldo, false, T, ld, nr, nl);
+  if (out_gl) copy_out(out_gl, ldo, false, A, ld, nl, nl);
+  // Caroli: Re Tr[(G gml)(G^H gmr)]
   copy_in(A, ld, opN<R>(c.gs[G_GML], ld), nl, nl);
   row_gemm<R, S>(nr, nl, nl, opN<R>(T, ld), opN<R>(A, ld), EpiStore<R>{U, ld, mk<R>(1, 0)});
   copy_in(A, ld, opN<R>(c.gs[G_GMR], ld), nr, nr);

@@ -1,0 +1,94 @@
+"""Mode-resolved transmission, CPU side: the oracle restatement of
+vel_mat_tdb against the reference's golden si-si sums, and the package's
+unfolding geometry against the oracle's."""
+import numpy as np
+import pytest
+
+from oracle import modes as M
+from oracle import negf as N
+from phinfortran_gb300.modes import LeadGeometry
+from tests.sisi_case import sisi_blocks, sisi_params
+
+SUMS = ("transl_s", "transl_ns", "transr_s", "transr_ns", "refll_s", "refll_ns", "reflr_s", "reflr_ns")
+
+
+def geometry(f):
+    nb = tuple(int(x) for x in f["n_bloch"])
+    b, p = int(f["buffer"]), int(f["period"])
+    return nb, M.lead_unfolding_setup(f["pos_all"], f["cell"], nb, b, p, b, p)
+
+
+def oracle_point_sums(f, ik, ies):
+    nb, (left, right) = geometry(f)
+    cell = f["cell"]
+    geom = dict(ksc=f["kgrid"][ik], recivec=2 * np.pi * np.linalg.inv(f["cell_all"]).T,
+                reci_uc_l=2 * np.pi * np.linalg.inv(cell).T, reci_uc_r=2 * np.pi * np.linalg.inv(cell).T,
+                a_z_l=cell[2, 2], a_z_r=cell[2, 2], left=left, right=right, pos_all=f["pos_all"], nb=nb)
+    p = sisi_params(f)
+    b = sisi_blocks(f, ik)
+    E = f["E"][ies]
+    r = N.transport(E, b, want_blocks=True, want_plus_minus=True, **p)
+    s = r["surface"]
+    out = []
+    for a, ie in enumerate(ies):
+        surf = {k: s[k][a] for k in ("gl_adv", "gr_ret", "gl_plus", "gr_minus", "gml_adv", "gmr_ret")}
+        rgf = {k: r[k][a] for k in ("G_D_RL", "G_D_LR", "G_L", "G_R")}
+        o = M.vel_mat_tdb(E[a], ie == 0, b, surf, rgf, geom, p["eta"], p["eta0"], 5e-3)
+        out.append((o, r["transl"][a]))
+    return out
+
+
+def test_oracle_modes_match_golden(sisi):
+    """Every sum within 1e-6 of the reference's output at points whose
+    propagating modes are non-degenerate, and the mode sum equal to the
+    Caroli T (velocity_mat.f90 vs lesser.f90)."""
+    f = sisi
+    for ik, ies in ((0, [0, 6, 20, 40]), (10, [12, 30]), (37, [5, 25, 50])):
+        for ie, (o, T) in zip(ies, oracle_point_sums(f, ik, ies)):
+            for k in SUMS:
+                assert abs(o[k] - f[k][ie, ik]) < 1e-6, (ik, ie, k, o[k], f[k][ie, ik])
+            assert abs(o["transl_s"] + o["transl_ns"] - T) < 1e-8 * max(1.0, T)
+
+
+def test_degenerate_gamma_point_split_is_basis_dependent(sisi):
+    """At the Gamma point of the 2x2-folded cell, degenerate Bloch modes of
+    different unfolded k share one eigenvalue; the s/ns split then depends
+    on the basis LAPACK picks inside the eigenspace.  The reference's own
+    outputs show it: transl_ns != transr_ns there.  Only the total is
+    fixed."""
+    f = sisi
+    ie, ik = 13, 24
+    assert abs(f["transl_ns"][ie, ik] - f["transr_ns"][ie, ik]) > 0.1
+    (o, T), = oracle_point_sums(f, ik, [ie])
+    g = f["transl_s"][ie, ik] + f["transl_ns"][ie, ik]
+    assert abs(o["transl_s"] + o["transl_ns"] - g) < 1e-6
+
+
+def test_package_geometry_matches_oracle(sisi):
+    f = sisi
+    nb, (left, right) = geometry(f)
+    b, p = int(f["buffer"]), int(f["period"])
+    g = LeadGeometry.from_qe(f["pos_all"], f["cell"], f["cell_all"], nb, b, p, b, p)
+    np.testing.assert_array_equal(g.list_l, left["list"])
+    np.testing.assert_array_equal(g.rep_l, left["pidx"])
+    np.testing.assert_array_equal(g.list_r, right["list"])
+    np.testing.assert_allclose(g.pos_r, right["pos"])
+    # unfolding weights through the phase table == the oracle's loop
+    rng = np.random.default_rng(3)
+    recivec = 2 * np.pi * np.linalg.inv(f["cell_all"]).T
+    reci_uc = 2 * np.pi * np.linalg.inv(f["cell"]).T
+    for ik in (0, 17, 24):
+        ksc = f["kgrid"][ik]
+        for side, lead in (("l", left), ("r", right)):
+            ph = g.phases(ksc, side)[0]
+            stride, nrep = g.layout(side)
+            u = rng.standard_normal(ph.shape[1]) + 1j * rng.standard_normal(ph.shape[1])
+            lam = np.exp(0.3j)
+            w_or = M.unfold_weights(u, lam, ksc, recivec, reci_uc, lead, f["pos_all"], nb)
+            nimg = ph.shape[1] // stride
+            w = np.zeros(ph.shape[0])
+            for js in range(ph.shape[0]):
+                for r0 in range(nrep):
+                    rows = r0 + stride * np.arange(nimg)
+                    w[js] += abs(np.sum(ph[js, rows] * u[rows] * lam)) ** 2 / nimg
+            np.testing.assert_allclose(w, w_or, rtol=1e-12)
