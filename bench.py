@@ -196,6 +196,50 @@ def time_steps(torch, fn, steps, flush, stream):
     return times
 
 
+def gradient_ratio(torch, flush, stream, steps):
+    """Adjoint gradient (d kappa / d every block) vs one forward sweep on the
+    simple-cubic 4x4x40 bar (n=48, L=40), masses U[1,3], springs U[0.8,1.2],
+    1024 frequencies, Landauer weights at T=300 (arb. units)."""
+    from phinfortran_gb300 import DeviceTransport, systems as S
+    from phinfortran_gb300.gradients import DeviceGradient, landauer_weights
+    b, E, p, aux = S.sc_phonon(nx=4, ny=4, L=40, ne=1024, mass_range=(1.0, 3.0), bond_range=(0.8, 1.2),
+                               seed_index=4)
+    Ed = torch.from_numpy(E).cuda()
+    w = torch.from_numpy(landauer_weights(aux["omega"], 300.0)).cuda()
+    f64 = DeviceTransport(b, E.size, precision="fp64", **p)
+    mix = DeviceTransport(b, E.size, precision="mixed", **p)
+    gr = DeviceGradient(b, E.size, ckpt=0, arith="df64", **p)
+    gr_all = DeviceGradient(b, E.size, ckpt=1, arith="df64", **p)
+    gr64 = DeviceGradient(b, E.size, ckpt=0, arith="fp64", **p)
+    out = {}
+    for name, fn in (("fwd_fp64", lambda: f64.run(Ed, stream=stream)), ("fwd_mixed", lambda: mix.run(Ed, stream=stream)),
+                     ("grad", lambda: gr.run(Ed, w, stream=stream)),
+                     ("grad_store_all", lambda: gr_all.run(Ed, w, stream=stream)),
+                     ("grad_fp64", lambda: gr64.run(Ed, w, stream=stream))):
+        fn()
+        torch.cuda.synchronize()
+        t = time_steps(torch, fn, steps, flush, stream)
+        out[name + "_ms"] = 1e3 * sum(t) / len(t)
+    Tg = gr.transl[:E.size].cpu().numpy()
+    T64 = f64.transl[:E.size].cpu().numpy()
+    torch.cuda.synchronize()
+    M = {k: v[0] for k, v in gr.sensitivities().items()}
+    M64 = {k: v[0] for k, v in gr64.sensitivities().items()}
+    dev = max(float(np.abs(M[k] - M64[k]).max() / max(np.abs(M64[k]).max(), 1e-300)) for k in M if M[k].size)
+    return dict(workload="simple-cubic phonon bar 4x4x40 (n=48, L=40), masses U[1,3], springs U[0.8,1.2], "
+                         "1024 omega, kappa at T=300",
+                grad_over_fwd_fp64=out["grad_ms"] / out["fwd_fp64_ms"],
+                grad_over_fwd_mixed=out["grad_ms"] / out["fwd_mixed_ms"],
+                grad_store_all_over_fwd_mixed=out["grad_store_all_ms"] / out["fwd_mixed_ms"],
+                grad_fp64_over_fwd_fp64=out["grad_fp64_ms"] / out["fwd_fp64_ms"],
+                grad_T_max_abs_dev_from_fp64=float(np.abs(Tg - T64).max()),
+                grad_sensitivity_max_rel_dev_df64_vs_fp64=dev,
+                note="grad = adjoint kernel in double-float arithmetic (forward T plus the weighted sensitivities "
+                     "of every device block) with the left-connected factors checkpointed every ceil(sqrt(L+2)) = 7 "
+                     "layers and recomputed; grad_store_all keeps every layer; grad_fp64 = the same checkpointed "
+                     "kernel in FP64", **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -209,6 +253,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the FP64 comparison path (accuracy and speed-up fields)")
+    ap.add_argument("--no-grad", action="store_true", help="skip the gradient / forward cost ratio")
     ap.add_argument("--energies", type=int, default=0,
                     help="use only N energies of the workload (profiling runs)")
     args = ap.parse_args()
@@ -292,6 +337,11 @@ def main():
                           note="points are 'fp64 reproducible' when a 1e-15 relative perturbation of the inputs "
                                "moves the FP64 result by <= 1e-10 relative"))
 
+    # ---- gradient cost vs forward cost on the differentiable-conductance workload ----
+    grad = None
+    if not args.no_grad:
+        grad = gradient_ratio(torch, flush, stream, max(1, min(args.steps, 2)))
+
     # ---- end to end through the host-pointer C entry ----
     nq, dims, arrs = TdbBlocks.from_dict(b).stacked()
     h2d = sum(fortran_block(v).nbytes for v in arrs.values()) + E.nbytes
@@ -361,7 +411,7 @@ def main():
                             l2="flushed (256 MB write) before every timed step", parallelism=f"replicas x{ws}"),
                 e2e=dict(value=e2e_value, unit="solves/s", h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
                          entry="pf_transport_tdb_mixed" if args.path == "mixed" else "pf_transport_tdb"),
-                roofline=roof, cpu_baseline=cpu, compare=compare,
+                roofline=roof, cpu_baseline=cpu, compare=compare, gradient=grad,
                 clocks=dict(sm_mhz=clk["sm_mhz"], sm_max_mhz=clk["sm_max_mhz"], reasons=clk["reasons"]),
                 gpu_launches=launches_per_step * args.steps, status_nonzero=int((status != 0).sum()))
     print(json.dumps(line), flush=True)

@@ -214,12 +214,23 @@ const char* pf_cond_last_error(void);
  * for the device blocks and the lead-device couplings:
  *   gHd [nq][L][n x n], gHdv [nq][L-1][n x n], gHld [nq][n x nl],
  *   gHrd [nq][n x nr]  (device arrays, interleaved complex, zeroed here).
- * The lead cells (HL, HLv, HR, HRv) are held fixed.  The cost is about
- * 2.6x one forward sweep (block LU, two block-column solves, contractions).
+ * The lead cells (HL, HLv, HR, HRv) are held fixed.
+ * ckpt: checkpoint interval of the left-connected factors.  0 picks
+ * ceil(sqrt(L + 2)): the factors and forward vectors are kept every ckpt
+ * layers and each segment is recomputed during the reverse pass (memory
+ * O(sqrt(L)) matrices per point in flight); 1 keeps every layer (memory
+ * O(L), no recomputation, less work).
+ * arith: PF_ARITH_FP64 (complex128 throughout) or PF_ARITH_DF64 (every
+ * block operation in double-float pairs on the FP32 pipe, ~48 significant
+ * bits; the blocks are converted once into the workspace).
  * work must hold pf_transport_tdb_grad_workspace_size(...) bytes.
  */
+#define PF_ARITH_FP64 0
+#define PF_ARITH_DF64 1
+
 size_t pf_transport_tdb_grad_workspace_size(int n, int nl, int nr, int L,
-                                            int nq, int npts);
+                                            int nq, int npts, int ckpt,
+                                            int arith);
 
 int pf_transport_tdb_grad_dev(int n, int nl, int nr, int L, int nq,
                               const double* HL, const double* HLv,
@@ -229,7 +240,8 @@ int pf_transport_tdb_grad_dev(int n, int nl, int nr, int L, int nq,
                               int npts, const double* E, const int* qidx,
                               const int* zero_flag, const double* weights,
                               double eta, double eta0, double dev_factor,
-                              double convergence, int max_iter,
+                              double convergence, int max_iter, int ckpt,
+                              int arith,
                               double* transl, int* status, int* iters,
                               double* gHd, double* gHdv, double* gHld,
                               double* gHrd, void* work, size_t work_bytes,

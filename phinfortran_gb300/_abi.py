@@ -58,12 +58,13 @@ SIGNATURES = {
     "pf_cond_last_error": (C.c_char_p, []),
     "pf_landauer_conductance": (C.c_int, [C.c_int, _dp, _dp, C.c_int, _dp, C.c_double, _dp]),
     "pf_grad_last_error": (C.c_char_p, []),
-    "pf_transport_tdb_grad_workspace_size": (C.c_size_t, [C.c_int] * 6),
+    "pf_transport_tdb_grad_workspace_size": (C.c_size_t, [C.c_int] * 8),
     "pf_transport_tdb_grad_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                            C.c_int, C.c_int,
                                             C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_size_t, C.c_void_p]),

@@ -25,22 +25,25 @@ struct EpiAtomic {
   int ld;
   double s;
   bool tconj;
-  __device__ __forceinline__ void operator()(int r, int c, cx<double> acc) const {
+  template <typename R>
+  __device__ __forceinline__ void operator()(int r, int c, cx<R> acc) const {
+    const double ax = to_d(acc.x), ay = to_d(acc.y);
     if (!tconj) {
-      atomicAdd(&dst[r + (size_t)c * ld].x, s * acc.x);
-      atomicAdd(&dst[r + (size_t)c * ld].y, s * acc.y);
+      atomicAdd(&dst[r + (size_t)c * ld].x, s * ax);
+      atomicAdd(&dst[r + (size_t)c * ld].y, s * ay);
     } else {
-      atomicAdd(&dst[c + (size_t)r * ld].x, s * acc.x);
-      atomicAdd(&dst[c + (size_t)r * ld].y, -s * acc.y);
+      atomicAdd(&dst[c + (size_t)r * ld].x, s * ax);
+      atomicAdd(&dst[c + (size_t)r * ld].y, -s * ay);
     }
   }
 };
+template <typename R>
 struct EpiAddStore {  // C = acc + Y
-  cx<double>* c;
+  cx<R>* c;
   int ld;
-  const cx<double>* y;
+  const cx<R>* y;
   int ldy;
-  __device__ __forceinline__ void operator()(int r, int col, cx<double> acc) const {
+  __device__ __forceinline__ void operator()(int r, int col, cx<R> acc) const {
     c[r + col * ld] = cadd(acc, y[r + col * ldy]);
   }
 };
@@ -52,37 +55,40 @@ struct GradOut {
   cx<double>* gHrd;  // [nq][n*nr]   (M for dHrd, n x nr)
 };
 
+template <typename R>
 struct GradSlabs {
-  cx<double>* lu;  // (L+2) factors
-  cx<double>* xs;  // (L+2) X blocks
-  cx<double>* ys;  // (L+2) forward Z vectors
-  cx<double>* k0;  // K_j
-  cx<double>* k1;  // K_{j+1}
+  cx<R>* lu;  // (L+2) factors
+  cx<R>* xs;  // (L+2) X blocks
+  cx<R>* ys;  // (L+2) forward Z vectors
+  cx<R>* k0;  // K_j
+  cx<R>* k1;  // K_{j+1}
   size_t mat;
 };
 
 // Operand V_j of the extended system (global, FP64 input layout).
-__device__ __forceinline__ Op<double> vop(const System<double>& s, int q, int j) {
+template <typename R>
+__device__ __forceinline__ Op<R> vop(const System<R>& s, int q, int j) {
   const int n = s.n, L = s.L;
-  if (j == 0) return opN<double>(s.Hld + (size_t)q * s.nl * n, s.nl);
-  if (j == L) return opC<double>(s.Hrd + (size_t)q * s.nr * n, s.nr);
-  return opN<double>(s.Hdv + ((size_t)q * (L - 1) + (j - 1)) * n * n, n);
+  if (j == 0) return opN<R>(s.Hld + (size_t)q * s.nl * n, s.nl);
+  if (j == L) return opC<R>(s.Hrd + (size_t)q * s.nr * n, s.nr);
+  return opN<R>(s.Hdv + ((size_t)q * (L - 1) + (j - 1)) * n * n, n);
 }
-__device__ __forceinline__ Op<double> vop_h(const System<double>& s, int q, int j) {
-  Op<double> o = vop(s, q, j);
+template <typename R>
+__device__ __forceinline__ Op<R> vop_h(const System<R>& s, int q, int j) {
+  Op<R> o = vop(s, q, j);
   o.ct = !o.ct;
   return o;
 }
-__device__ __forceinline__ int xdim(const System<double>& s, int j) {
+template <typename R>
+__device__ __forceinline__ int xdim(const System<R>& s, int j) {
   return j == 0 ? s.nl : (j == s.L + 1 ? s.nr : s.n);
 }
 
 // Forward T and the weighted sensitivities of one point.  Lead results are
 // expected in scratch (lead_pair).  Returns status bits; *trans = T.
-template <int S>
-__device__ int adjoint_point(const Ctx<double>& c, const System<double>& sys, int q, cx<double> zD, double w,
-                             const GradSlabs& sl, const GradOut& go, double* trans) {
-  using R = double;
+template <typename R, int S>
+__device__ int adjoint_point(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, double w,
+                             const GradSlabs<R>& sl, const GradOut& go, double* trans) {
   const int ld = c.ld, L = sys.L, n = sys.n, nl = sys.nl, nr = sys.nr;
   const size_t mat = sl.mat;
   int st = PF_OK;
@@ -159,7 +165,7 @@ __device__ int adjoint_point(const Ctx<double>& c, const System<double>& sys, in
       const int dn = xdim(sys, j + 1);
       row_gemm<R, S>(dj, nl, dn, vop(sys, q, j), opN<R>(sZn, ld), EpiStore<R>{s1, ld, mk<R>(1, 0)});
       row_gemm<R, S>(dj, nl, dj, opC<R>(sl.lu + j * mat, ld), opN<R>(s1, ld),
-                     EpiAddStore{sZ, ld, sl.ys + j * mat, ld});
+                     EpiAddStore<R>{sZ, ld, sl.ys + j * mat, ld});
     }
     // K_j = X_j W  (dj x nl)
     row_gemm<R, S>(dj, nl, nr, opN<R>(sl.xs + j * mat, ld), opN<R>(sW, ld), EpiStore<R>{kc, ld, mk<R>(1, 0)});
@@ -169,7 +175,7 @@ __device__ int adjoint_point(const Ctx<double>& c, const System<double>& sys, in
     }
     if (j <= L) {  // M_V_j = 2w (K_{j+1} Z_j^H + (K_j Z_{j+1}^H)^H)  (d_{j+1} x d_j)
       const int dn = xdim(sys, j + 1);
-      cx<R>* dst;
+      cx<double>* dst;
       int ldd;
       bool hconj;  // V_L = Hrd^H: accumulate M_V_L^H into gHrd
       if (j == 0) {
@@ -195,6 +201,178 @@ __device__ int adjoint_point(const Ctx<double>& c, const System<double>& sys, in
     cx<R>* u = kn;
     kn = kc;
     kc = u;
+  }
+  return st;
+}
+
+// ---------------------------------------------------------------------------
+// Checkpointed variant: memory O(sqrt(L)) instead of O(L) per point.
+//
+// Pass A (j = 0..L+1) forms the left-connected factors g_j, the forward
+// vectors y_j and the left-connected propagation G0_j = G^L_{0,j}
+// (G0_{L+1} = X_0), keeping (g_j, y_j) only at the checkpoints j = k*seg.
+// Pass B walks the segments from the right: it recomputes the segment's
+// g_j, y_j from its checkpoint and, layer by layer downwards, forms
+// X_j = g_j V_j X_{j+1}, Z_j = y_j + g_j^H V_j Z_{j+1}, K_j = X_j W and the
+// sensitivities.  Extra work over the store-all kernel: one recomputation
+// of the factors and the y vectors, plus the G0 propagation.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct CkptSlabs {
+  cx<R>* ckg;   // [K] checkpoint factors
+  cx<R>* cky;   // [K] checkpoint y vectors
+  cx<R>* segg;  // [seg] segment factors
+  cx<R>* segy;  // [seg] segment y vectors
+  cx<R>* pg;    // pass A rolling g
+  cx<R>* py;    // pass A rolling y
+  cx<R>* pG0;   // pass A rolling G0 (ends as X_0)
+  cx<R>* W;     // Gamma_R X_0^H Gamma_L
+  cx<R>* xa;    // X rolling pair
+  cx<R>* xb;
+  cx<R>* k0;    // K rolling pair
+  cx<R>* k1;
+  size_t mat;
+  int seg;
+};
+
+// g_j and y_j from g_{j-1}, y_{j-1} (global).  Slots: V -> sv, g V -> sgv,
+// the inverted block -> sg; y_j written to ydst, g_j to gdst (global).
+template <typename R, int S>
+__device__ int ckpt_step(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, int j, const cx<R>* gprev,
+                         const cx<R>* yprev, cx<R>* sv, cx<R>* sgv, cx<R>* sg, cx<R>* gdst, cx<R>* ydst) {
+  const int ld = c.ld, L = sys.L, n = sys.n, nl = sys.nl, nr = sys.nr;
+  const int dp = xdim(sys, j - 1), dj = xdim(sys, j);
+  Op<R> none = opN<R>(nullptr, 1);
+  copy_in(sv, ld, vop(sys, q, j - 1), dp, dj);
+  row_gemm<R, S>(dp, dj, dp, opN<R>(gprev, ld), opN<R>(sv, ld), EpiStore<R>{sgv, ld, mk<R>(1, 0)});
+  EpiShift<R> e;
+  e.c = sg;
+  e.ld = ld;
+  e.z = zD;
+  if (j <= L) {
+    e.h = opN<R>(sys.Hd + ((size_t)q * L + (j - 1)) * n * n, n);
+    e.has_h = true;
+    e.s = none;
+    e.has_s = false;
+  } else {
+    e.h = opN<R>(sys.HR + (size_t)q * nr * nr, nr);
+    e.has_h = true;
+    e.s = opN<R>(c.gs[G_SR], ld);
+    e.has_s = true;
+  }
+  row_gemm<R, S>(dj, dj, dp, opC<R>(sv, ld), opN<R>(sgv, ld), e);
+  const int st = inverse(sg, ld, dj, c.iw);
+  // y_j = g_j^H (V^H y_{j-1})
+  row_gemm<R, S>(dj, nl, dp, opC<R>(sv, ld), opN<R>(yprev, ld), EpiStore<R>{sgv, ld, mk<R>(1, 0)});
+  row_gemm<R, S>(dj, nl, dj, opC<R>(sg, ld), opN<R>(sgv, ld), EpiStore<R>{ydst, ld, mk<R>(1, 0)});
+  if (gdst) copy_out(gdst, ld, false, sg, ld, dj, dj);
+  return st;
+}
+
+template <typename R, int S>
+__device__ int adjoint_point_ckpt(const Ctx<R>& c, const System<R>& sys, int q, cx<R> zD, double w,
+                                  const CkptSlabs<R>& sl, const GradOut& go, double* trans) {
+  const int ld = c.ld, L = sys.L, n = sys.n, nl = sys.nl, nr = sys.nr;
+  const size_t mat = sl.mat;
+  const int seg = sl.seg;
+  int st = PF_OK;
+  cx<R>* s0 = c.sm[0];
+  cx<R>* s1 = c.sm[1];
+  cx<R>* s2 = c.sm[2];
+  cx<R>* s3 = c.sm[3];
+  // ---- pass A
+  copy_in(sl.pg, ld, opN<R>(c.gs[G_GL], ld), nl, nl);
+  copy_in(sl.py, ld, opC<R>(c.gs[G_GL], ld), nl, nl);
+  copy_in(sl.pG0, ld, opN<R>(c.gs[G_GL], ld), nl, nl);
+  copy_in(sl.ckg, ld, opN<R>(c.gs[G_GL], ld), nl, nl);
+  copy_in(sl.cky, ld, opC<R>(c.gs[G_GL], ld), nl, nl);
+  for (int j = 1; j <= L + 1; ++j) {
+    const int dj = xdim(sys, j);
+    // s0 = V_{j-1}, s1 = scratch, s2 = g_j; y_j -> py (its product reads s1, not py)
+    st |= ckpt_step<R, S>(c, sys, q, zD, j, sl.pg, sl.py, s0, s1, s2, nullptr, s3);
+    copy_out(sl.py, ld, false, s3, ld, dj, nl);
+    // G0_j = (G0_{j-1} V_{j-1}) g_j
+    row_gemm<R, S>(nl, dj, xdim(sys, j - 1), opN<R>(sl.pG0, ld), opN<R>(s0, ld), EpiStore<R>{s1, ld, mk<R>(1, 0)});
+    row_gemm<R, S>(nl, dj, dj, opN<R>(s1, ld), opN<R>(s2, ld), EpiStore<R>{sl.pG0, ld, mk<R>(1, 0)});
+    copy_out(sl.pg, ld, false, s2, ld, dj, dj);
+    if (j % seg == 0) {
+      copy_out(sl.ckg + (size_t)(j / seg) * mat, ld, false, s2, ld, dj, dj);
+      copy_out(sl.cky + (size_t)(j / seg) * mat, ld, false, s3, ld, dj, nl);
+    }
+  }
+  // ---- T and W from X_0 = G0_{L+1}
+  copy_in(s0, ld, opN<R>(c.gs[G_GMR], ld), nr, nr);
+  row_gemm<R, S>(nl, nr, nr, opN<R>(sl.pG0, ld), opN<R>(s0, ld), EpiStore<R>{s1, ld, mk<R>(1, 0)});  // P
+  copy_in(s2, ld, opN<R>(c.gs[G_GML], ld), nl, nl);
+  row_gemm<R, S>(nr, nl, nl, opC<R>(sl.pG0, ld), opN<R>(s2, ld), EpiStore<R>{s3, ld, mk<R>(1, 0)});  // Q
+  *trans = trace_prod_re(s1, ld, opN<R>(s3, ld), nl, nr, c.red);
+  row_gemm<R, S>(nr, nl, nr, opN<R>(s0, ld), opN<R>(s3, ld), EpiStore<R>{sl.W, ld, mk<R>(1, 0)});  // W
+  // ---- pass B
+  const double s2w = 2.0 * w;
+  cx<R>* sZ = s3;
+  cx<R>* sZn = s0;
+  cx<R>* xc = sl.xa;
+  cx<R>* xn = sl.xb;
+  cx<R>* kc = sl.k0;
+  cx<R>* kn = sl.k1;
+  const int nseg = (L + 2 + seg - 1) / seg;
+  for (int k = nseg - 1; k >= 0; --k) {
+    const int c0 = k * seg;
+    const int e = (c0 + seg < L + 2) ? c0 + seg : L + 2;
+    // recompute the segment's factors and y vectors (slots: s1, s2 and the free Z slot)
+    copy_in(sl.segg, ld, opN<R>(sl.ckg + (size_t)k * mat, ld), xdim(sys, c0), xdim(sys, c0));
+    copy_in(sl.segy, ld, opN<R>(sl.cky + (size_t)k * mat, ld), xdim(sys, c0), nl);
+    for (int j = c0 + 1; j < e; ++j) {
+      const int i = j - c0;
+      st |= ckpt_step<R, S>(c, sys, q, zD, j, sl.segg + (size_t)(i - 1) * mat, sl.segy + (size_t)(i - 1) * mat, s1, s2,
+                         sZ, sl.segg + (size_t)i * mat, sl.segy + (size_t)i * mat);
+    }
+    for (int j = e - 1; j >= c0; --j) {
+      const int dj = xdim(sys, j);
+      const cx<R>* gj = sl.segg + (size_t)(j - c0) * mat;
+      const cx<R>* yj = sl.segy + (size_t)(j - c0) * mat;
+      if (j == L + 1) {
+        copy_in(xc, ld, opN<R>(gj, ld), nr, nr);
+        copy_in(sZ, ld, opN<R>(yj, ld), dj, nl);
+      } else {
+        const int dn = xdim(sys, j + 1);
+        row_gemm<R, S>(dj, nr, dn, vop(sys, q, j), opN<R>(xn, ld), EpiStore<R>{s1, ld, mk<R>(1, 0)});
+        row_gemm<R, S>(dj, nr, dj, opN<R>(gj, ld), opN<R>(s1, ld), EpiStore<R>{xc, ld, mk<R>(1, 0)});
+        row_gemm<R, S>(dj, nl, dn, vop(sys, q, j), opN<R>(sZn, ld), EpiStore<R>{s1, ld, mk<R>(1, 0)});
+        row_gemm<R, S>(dj, nl, dj, opC<R>(gj, ld), opN<R>(s1, ld), EpiAddStore<R>{sZ, ld, yj, ld});
+      }
+      row_gemm<R, S>(dj, nl, nr, opN<R>(xc, ld), opN<R>(sl.W, ld), EpiStore<R>{kc, ld, mk<R>(1, 0)});
+      if (j >= 1 && j <= L) {
+        row_gemm<R, S>(dj, dj, nl, opN<R>(kc, ld), opC<R>(sZ, ld),
+                       EpiAtomic{go.gHd + ((size_t)q * L + (j - 1)) * n * n, n, s2w, false});
+      }
+      if (j <= L) {
+        const int dn = xdim(sys, j + 1);
+        cx<double>* dst;
+        bool hconj;
+        if (j == 0) {
+          dst = go.gHld + (size_t)q * n * nl;
+          hconj = false;
+        } else if (j == L) {
+          dst = go.gHrd + (size_t)q * n * nr;
+          hconj = true;
+        } else {
+          dst = go.gHdv + ((size_t)q * (L - 1) + (j - 1)) * n * n;
+          hconj = false;
+        }
+        row_gemm<R, S>(dn, dj, nl, opN<R>(kn, ld), opC<R>(sZ, ld), EpiAtomic{dst, n, s2w, hconj});
+        row_gemm<R, S>(dj, dn, nl, opN<R>(kc, ld), opC<R>(sZn, ld), EpiAtomic{dst, n, s2w, !hconj});
+      }
+      cx<R>* t = sZn;
+      sZn = sZ;
+      sZ = t;
+      cx<R>* u = xn;
+      xn = xc;
+      xc = u;
+      cx<R>* v = kn;
+      kn = kc;
+      kc = v;
+    }
   }
   return st;
 }

@@ -10,9 +10,11 @@
 #include <stdio.h>
 
 #include "../../include/phinfortran_gb300.h"
-#include "adjoint.cuh"
+#include "grad_impl.cuh"
 
 using pf::cx;
+using pfgrad::GLayout;
+using pfgrad::glayout;
 
 namespace {
 
@@ -31,100 +33,12 @@ int cuda_err(cudaError_t e, const char* where) {
     if (e_ != cudaSuccess) return cuda_err(e_, #call); \
   } while (0)
 
-constexpr int kThreads = 256;
-
-struct GLayout {
-  int m, ld;
-  size_t mat, smem, per_cta;
-};
-
-GLayout glayout(int n, int nl, int nr, int L) {
-  GLayout g;
-  g.m = n > nl ? n : nl;
-  g.m = g.m > nr ? g.m : nr;
-  g.ld = g.m | 1;
-  g.mat = (size_t)g.ld * g.m;
-  g.smem = pf::NSM * g.mat * 16 + 32 * sizeof(double) + 2 * (size_t)g.m * 16 + (size_t)g.m * 4 + 64 * 4;
-  g.per_cta = ((size_t)pf::NG * g.mat * 16 + (3 * (size_t)(L + 2) + 2) * g.mat * 16 + 255) & ~(size_t)255;
-  return g;
-}
-
-template <int S>
-__global__ void __launch_bounds__(kThreads) grad_kernel(pf::System<double> sys, pf::Points pts, pf::Params P,
-                                                        const double* weights, pf::Outputs out, pf::GradOut go,
-                                                        GLayout lay, char* scratch, int* queue) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  pf::Ctx<double> c;
-  cx<double>* s = reinterpret_cast<cx<double>*>(smem_raw);
-  for (int i = 0; i < pf::NSM; ++i) c.sm[i] = s + i * lay.mat;
-  unsigned char* tail = reinterpret_cast<unsigned char*>(s + pf::NSM * lay.mat);
-  c.red = reinterpret_cast<double*>(tail);
-  c.iw.rowk = reinterpret_cast<cx<double>*>(tail + 32 * sizeof(double));
-  c.iw.colk = c.iw.rowk + lay.m;
-  int* ip = reinterpret_cast<int*>(c.iw.colk + lay.m);
-  c.iw.perm = ip;
-  c.iw.flag = ip + lay.m;
-  cx<double>* g = reinterpret_cast<cx<double>*>(scratch + (size_t)blockIdx.x * lay.per_cta);
-  for (int i = 0; i < pf::NG; ++i) c.gs[i] = g + i * lay.mat;
-  c.ld = lay.ld;
-  pf::GradSlabs sl;
-  sl.mat = lay.mat;
-  sl.lu = g + pf::NG * lay.mat;
-  sl.xs = sl.lu + (size_t)(sys.L + 2) * lay.mat;
-  sl.ys = sl.xs + (size_t)(sys.L + 2) * lay.mat;
-  sl.k0 = sl.ys + (size_t)(sys.L + 2) * lay.mat;
-  sl.k1 = sl.k0 + lay.mat;
-  __shared__ int s_p;
-  for (;;) {
-    if (threadIdx.x == 0) s_p = atomicAdd(queue, 1);
-    __syncthreads();
-    const int p = s_p;
-    __syncthreads();
-    if (p >= pts.npts) break;
-    const int q = pts.qidx ? pts.qidx[p] : 0;
-    const double E = pts.E[p];
-    int itl = 0, itr = 0;
-    int st = pf::lead_pair<double, S>(c, sys, q, E, P, &itl, &itr);
-    const double eps = E * P.eta + P.eta0;
-    const cx<double> zD = pf::mk<double>(E, P.dev_factor * eps);
-    const bool zero = pts.zero_flag && pts.zero_flag[p];
-    const double w = (weights ? weights[p] : 1.0) * (zero ? 0.0 : 1.0);
-    double tl = 0.0;
-    st |= pf::adjoint_point<S>(c, sys, q, zD, w, sl, go, &tl);
-    if (threadIdx.x == 0) {
-      double a = tl;
-      if (zero || a < 1.0e-60) a = 0.0;
-      out.transl[p] = a;
-      out.status[p] = st;
-      if (out.iters) {
-        out.iters[2 * p] = itl;
-        out.iters[2 * p + 1] = itr;
-      }
-    }
-    __syncthreads();
-  }
-}
-
-int grad_grid(const GLayout& lay, int npts, int S) {
-  int dev = 0, sms = 0, per_sm = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return -1;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (S == 1) {
-    if (cudaFuncSetAttribute(grad_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.smem) !=
-        cudaSuccess)
-      return -1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grad_kernel<1>, kThreads, lay.smem) != cudaSuccess)
-      return -1;
-  } else {
-    if (cudaFuncSetAttribute(grad_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.smem) !=
-        cudaSuccess)
-      return -1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grad_kernel<2>, kThreads, lay.smem) != cudaSuccess)
-      return -1;
-  }
-  if (per_sm < 1) return -1;
-  const int g = sms * per_sm;
-  return g < npts ? g : npts;
+// bytes of the double-float copy of the blocks (0 for FP64)
+size_t df64_blocks_bytes(int n, int nl, int nr, int L, int nq, int arith) {
+  if (arith != PF_ARITH_DF64) return 0;
+  const size_t c = (size_t)nq * (2 * (size_t)nl * nl + 2 * (size_t)nr * nr + (size_t)L * n * n +
+                                 (size_t)(L > 1 ? L - 1 : 0) * n * n + (size_t)nl * n + (size_t)nr * n);
+  return ((c * 16) + 255) & ~(size_t)255;
 }
 
 // lead mirror flags (same rule as the transport entry)
@@ -151,21 +65,24 @@ extern "C" {
 
 const char* pf_grad_last_error(void) { return g_err; }
 
-size_t pf_transport_tdb_grad_workspace_size(int n, int nl, int nr, int L, int nq, int npts) {
-  if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0) return 0;
+size_t pf_transport_tdb_grad_workspace_size(int n, int nl, int nr, int L, int nq, int npts, int ckpt,
+                                            int arith) {
+  if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0 || ckpt < 0) return 0;
+  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64) return 0;
   if (n > PF_NMAX_RESIDENT || nl > PF_NMAX_RESIDENT || nr > PF_NMAX_RESIDENT) return 0;
-  GLayout lay = glayout(n, nl, nr, L);
-  const int S = (lay.m + 31) / 32;
-  const int g = grad_grid(lay, npts > 0 ? npts : 1, S);
+  GLayout lay = glayout(n, nl, nr, L, ckpt);
+  const int np = npts > 0 ? npts : 1;
+  const int g = arith == PF_ARITH_FP64 ? pfgrad::grid_fp64(lay, np) : pfgrad::grid_df64(lay, np);
   if (g <= 0) return 0;
-  return 256 + (((size_t)nq * 4 + 255) & ~(size_t)255) + (size_t)g * lay.per_cta;
+  return 256 + (((size_t)nq * 4 + 255) & ~(size_t)255) + (size_t)g * lay.per_cta + df64_blocks_bytes(n, nl, nr, L, nq, arith);
 }
 
 int pf_transport_tdb_grad_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
                               const double* HR, const double* HRv, const double* Hd, const double* Hdv,
                               const double* Hld, const double* Hrd, int npts, const double* E, const int* qidx,
                               const int* zero_flag, const double* weights, double eta, double eta0,
-                              double dev_factor, double convergence, int max_iter, double* transl, int* status,
+                              double dev_factor, double convergence, int max_iter, int ckpt, int arith,
+                              double* transl, int* status,
                               int* iters, double* gHd, double* gHdv, double* gHld, double* gHrd, void* work,
                               size_t work_bytes, void* stream) {
   if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0)
@@ -177,6 +94,8 @@ int pf_transport_tdb_grad_dev(int n, int nl, int nr, int L, int nq, const double
   if (!HL || !HLv || !HR || !HRv || !Hd || !Hld || !Hrd || (L > 1 && !Hdv))
     return set_err(PF_ERR_ARG, "pf_grad: null block pointer");
   if (max_iter <= 0) return set_err(PF_ERR_ARG, "pf_grad: max_iter must be positive");
+  if (ckpt < 0) return set_err(PF_ERR_ARG, "pf_grad: checkpoint interval must be >= 0");
+  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64) return set_err(PF_ERR_ARG, "pf_grad: unknown arithmetic");
   cudaStream_t st = (cudaStream_t)stream;
   // zero the accumulators
   GR_CUDA(cudaMemsetAsync(gHd, 0, (size_t)nq * L * n * n * 16, st));
@@ -184,12 +103,12 @@ int pf_transport_tdb_grad_dev(int n, int nl, int nr, int L, int nq, const double
   GR_CUDA(cudaMemsetAsync(gHld, 0, (size_t)nq * n * nl * 16, st));
   GR_CUDA(cudaMemsetAsync(gHrd, 0, (size_t)nq * n * nr * 16, st));
   if (npts == 0) return PF_SUCCESS;
-  GLayout lay = glayout(n, nl, nr, L);
-  const int S = (lay.m + 31) / 32;
-  const int grid = grad_grid(lay, npts, S);
+  GLayout lay = glayout(n, nl, nr, L, ckpt);
+  const int grid = arith == PF_ARITH_FP64 ? pfgrad::grid_fp64(lay, npts) : pfgrad::grid_df64(lay, npts);
   if (grid <= 0) return set_err(PF_ERR_SIZE, "pf_grad: kernel does not fit on the device");
   const size_t mir = ((size_t)nq * 4 + 255) & ~(size_t)255;
-  if (!work || work_bytes < 256 + mir + (size_t)grid * lay.per_cta)
+  const size_t dfb = df64_blocks_bytes(n, nl, nr, L, nq, arith);
+  if (!work || work_bytes < 256 + mir + (size_t)grid * lay.per_cta + dfb)
     return set_err(PF_ERR_ARG, "pf_grad: workspace too small");
   int* queue = reinterpret_cast<int*>(work);
   int* mirror = reinterpret_cast<int*>(reinterpret_cast<char*>(work) + 256);
@@ -221,10 +140,11 @@ int pf_transport_tdb_grad_dev(int n, int nl, int nr, int L, int nq, const double
   go.gHdv = reinterpret_cast<cx<double>*>(gHdv);
   go.gHld = reinterpret_cast<cx<double>*>(gHld);
   go.gHrd = reinterpret_cast<cx<double>*>(gHrd);
-  if (S == 1)
-    grad_kernel<1><<<grid, kThreads, lay.smem, st>>>(sys, pts, P, weights, out, go, lay, scratch, queue);
+  if (arith == PF_ARITH_FP64)
+    pfgrad::launch_fp64(grid, lay, sys, pts, P, weights, out, go, scratch, queue, st);
   else
-    grad_kernel<2><<<grid, kThreads, lay.smem, st>>>(sys, pts, P, weights, out, go, lay, scratch, queue);
+    pfgrad::launch_df64(grid, lay, sys, reinterpret_cast<pf::df64*>(scratch + (size_t)grid * lay.per_cta), pts, P,
+                        weights, out, go, scratch, queue, st);
   GR_CUDA(cudaGetLastError());
   return PF_SUCCESS;
 }

@@ -22,6 +22,7 @@ from .transport import BLOCK_NAMES, TdbBlocks, fortran_block
 KB = 1.380649e-23
 HBAR = 1.0545718e-34
 THZ2RADS = 1e12 * np.pi * 2
+ARITH = {"fp64": 0, "df64": 1}   # PF_ARITH_FP64, PF_ARITH_DF64
 
 
 def _unpack(buf, shape):
@@ -36,7 +37,7 @@ class DeviceGradient:
     launches; ``run`` takes device-resident energies and weights."""
 
     def __init__(self, blocks, npts_max, *, eta, eta0, convergence, dev_factor=10.0, max_iter=1000,
-                 device="cuda"):
+                 ckpt=0, arith="fp64", device="cuda"):
         import torch
         self.torch = torch
         lib = _abi.load()
@@ -46,11 +47,15 @@ class DeviceGradient:
         self.dims = (n, nl, nr, L, nq)
         self.dev = {k: torch.from_numpy(fortran_block(v).copy()).to(device) for k, v in arrs.items()}
         self.params = (eta, eta0, dev_factor, convergence, max_iter)
+        self.ckpt = int(ckpt)
+        if arith not in ARITH:
+            raise ValueError(f"arith must be one of {sorted(ARITH)}")
+        self.arith = ARITH[arith]
         self.npts_max = npts_max
         self.shapes = dict(Hd=(nq, L, n, n), Hdv=(nq, max(L - 1, 0), n, n), Hld=(nq, n, nl), Hrd=(nq, n, nr))
         self.g = {k: torch.zeros(max(2 * int(np.prod(s)), 2), dtype=torch.float64, device=device)
                   for k, s in self.shapes.items()}
-        ws = lib.pf_transport_tdb_grad_workspace_size(n, nl, nr, L, nq, npts_max)
+        ws = lib.pf_transport_tdb_grad_workspace_size(n, nl, nr, L, nq, npts_max, self.ckpt, self.arith)
         if ws == 0:
             raise _abi.PFError(-3, "gradient kernel does not fit (block size > 48?)")
         self.work = torch.empty(ws, dtype=torch.uint8, device=device)
@@ -71,7 +76,8 @@ class DeviceGradient:
         g = self.g
         rc = lib.pf_transport_tdb_grad_dev(n, nl, nr, L, nq, *[self.dev[k].data_ptr() for k in BLOCK_NAMES],
                                            npts, E.data_ptr(), p(qidx), p(zero_flag), p(weights), eta, eta0,
-                                           dev_factor, conv, max_iter, self.transl.data_ptr(),
+                                           dev_factor, conv, max_iter, self.ckpt, self.arith,
+                                           self.transl.data_ptr(),
                                            self.status.data_ptr(), self.iters.data_ptr(), g["Hd"].data_ptr(),
                                            g["Hdv"].data_ptr() if L > 1 else None, g["Hld"].data_ptr(),
                                            g["Hrd"].data_ptr(), self.work.data_ptr(), self.work.numel(),
@@ -86,12 +92,12 @@ class DeviceGradient:
 
 
 def transport_grad(E, blocks, weights=None, *, eta, eta0, convergence, dev_factor=10.0, qidx=None,
-                   zero_flag=None, max_iter=1000, check=True):
+                   zero_flag=None, max_iter=1000, ckpt=0, arith="fp64", check=True):
     """Forward T (npts,) and M dict (leading q axis) through the adjoint kernel."""
     import torch
     E = np.ascontiguousarray(E, dtype=np.float64)
     dg = DeviceGradient(blocks, max(E.size, 1), eta=eta, eta0=eta0, convergence=convergence,
-                        dev_factor=dev_factor, max_iter=max_iter)
+                        dev_factor=dev_factor, max_iter=max_iter, ckpt=ckpt, arith=arith)
     dev = lambda a, dt: None if a is None else torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).cuda()
     tl, st = dg.run(dev(E, np.float64), dev(weights, np.float64), dev(qidx, np.int32), dev(zero_flag, np.int32))
     torch.cuda.synchronize()
@@ -122,11 +128,14 @@ def _torch_function():
     class ConductanceFunction(torch.autograd.Function):
         """kappa(masses, springs) of an ScBar; backward through the adjoint kernel.
 
-        forward(masses, springs, bar, omega, temperature, params, precision)
+        forward(masses, springs, bar, omega, temperature, params, precision, grad_arith, ckpt)
+        precision: forward path ("fp64" or "mixed"); grad_arith: "fp64" or
+        "df64" for the adjoint; ckpt: checkpoint interval (0 = sqrt(L+2)).
         """
 
         @staticmethod
-        def forward(ctx, masses, springs, bar, omega, temperature, params, precision="fp64"):
+        def forward(ctx, masses, springs, bar, omega, temperature, params, precision="fp64", grad_arith="df64",
+                    ckpt=0):
             from .transport import transport_tdb
             m = masses.detach().cpu().numpy().astype(np.float64)
             k = springs.detach().cpu().numpy().astype(np.float64)
@@ -136,6 +145,7 @@ def _torch_function():
             r = transport_tdb(E, blocks, want_transr=False, precision=precision, **params)
             ctx.save_for_backward(masses, springs)
             ctx.bar, ctx.E, ctx.wts, ctx.params = bar, E, wts, params
+            ctx.grad_arith, ctx.ckpt = grad_arith, ckpt
             return torch.tensor(float(np.dot(wts, r["transl"])), dtype=torch.float64)
 
         @staticmethod
@@ -144,12 +154,12 @@ def _torch_function():
             m = masses.detach().cpu().numpy().astype(np.float64)
             k = springs.detach().cpu().numpy().astype(np.float64)
             blocks = ctx.bar.blocks(m, k)
-            _, M, _ = transport_grad(ctx.E, blocks, ctx.wts, **ctx.params)
+            _, M, _ = transport_grad(ctx.E, blocks, ctx.wts, ckpt=ctx.ckpt, arith=ctx.grad_arith, **ctx.params)
             GD = ctx.bar.sensitivity_matrix({kk: v[0] for kk, v in M.items()})
             gm, gk = ctx.bar.parameter_gradient(GD, m, k)
             g = float(grad_out)
             return (torch.from_numpy(gm * g).to(masses), torch.from_numpy(gk * g).to(springs),
-                    None, None, None, None, None)
+                    None, None, None, None, None, None, None)
 
     return ConductanceFunction
 
