@@ -328,6 +328,37 @@ int pf_transport_tdb_modes_dev(int n, int nl, int nr, int L, int nq,
 /* Message for the last error of the mode-resolved entry point. */
 const char* pf_modes_last_error(void);
 
+/*
+ * Large-block transport (FP64): the same quantities as
+ * pf_transport_tdb_dev with want_transr = 0 (T_L, status, iterations) for
+ * block sizes above PF_NMAX_RESIDENT, up to PF_NMAX_TILED.  Replaces the
+ * same reference calls as pf_transport_tdb_dev (surface_green_tdb_mpi,
+ * negf/surface.f90:344-383, and get_G_full_tdb_mpi, negf/lesser.f90:100-157)
+ * for cross-sections whose blocks do not fit in shared memory.  Points are
+ * grouped by q and advanced in batches through batched tile kernels (block
+ * GEMMs, a blocked Gauss-Jordan inverse, masked decimation steps).  The call
+ * is synchronous with respect to `stream` (the decimation loop reads one
+ * counter per step).  work: pf_transport_tdb_tiled_workspace_size bytes.
+ */
+#define PF_NMAX_TILED 2048
+
+size_t pf_transport_tdb_tiled_workspace_size(int n, int nl, int nr, int nq, int npts);
+
+int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq,
+                               const double* HL, const double* HLv,
+                               const double* HR, const double* HRv,
+                               const double* Hd, const double* Hdv,
+                               const double* Hld, const double* Hrd,
+                               int npts, const double* E, const int* qidx,
+                               const int* zero_flag,
+                               double eta, double eta0, double dev_factor,
+                               double convergence, int max_iter,
+                               double* transl, int* status, int* iters,
+                               void* work, size_t work_bytes, void* stream);
+
+/* Message for the last error of the large-block entry points. */
+const char* pf_tiled_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

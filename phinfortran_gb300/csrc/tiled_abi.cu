@@ -1,0 +1,604 @@
+// extern "C" entry of the large-block transport path (block sizes above the
+// shared-memory resident kernels: the diamond slabs with n = 96..384 DOF
+// per layer, the 3-orbital ribbons with n = 768).
+//
+// Points are grouped by q (their blocks are then shared operands) and run
+// in batches that advance together: the Lopez-Sancho decimations of the
+// two leads (surface.f90:479-568) with a per-point convergence mask, the
+// left-to-right RGF sweep (lesser.f90:547-654) and the Caroli trace
+// (lesser.f90:787-800).  Every step is one launch over the batch (tiled.cuh);
+// the host only drives the loop and reads one counter per decimation step.
+#include <cuda_runtime.h>
+#include <stdio.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "../../include/phinfortran_gb300.h"
+#include "tiled.cuh"
+#include "transport.cuh"
+
+using pf::cx;
+using namespace pf::tiled;
+
+namespace {
+
+thread_local char g_err[512] = "";
+int set_err(int code, const char* msg) {
+  snprintf(g_err, sizeof(g_err), "%s", msg);
+  return code;
+}
+int cuda_err(cudaError_t e, const char* where) {
+  snprintf(g_err, sizeof(g_err), "%s: %s", where, cudaGetErrorString(e));
+  return PF_ERR_CUDA;
+}
+#define TL_CUDA(call)                                  \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_err(e_, #call); \
+  } while (0)
+
+constexpr int kMaxBatch = 256;
+constexpr size_t kBatchBytes = (size_t)6 << 30;
+constexpr size_t kSmallInvBytes = 200 * 1024;
+constexpr size_t kPanelBytes = 200 * 1024;
+constexpr int kMats = 16;  // per-point working matrices
+
+// complex constant for host code (pf::mk is device-only)
+template <typename T>
+__host__ __device__ inline cx<T> hmk(T a, T b) {
+  cx<T> z;
+  z.x = a;
+  z.y = b;
+  return z;
+}
+
+// ---------------------------------------------------------------------------
+// elementwise kernels (grid: (ceil(m*m/256), batch))
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_shift_neg(cx<T>* dst, const cx<T>* src, long long stride, int m, int ld, const cx<T>* z,
+                            const int* active) {
+  const int b = blockIdx.y;
+  if (active && !active[b]) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m * m) return;
+  const int r = i % m, c = i / m;
+  cx<T> v = src[(size_t)b * stride + r + (size_t)c * ld];
+  v = pf::mk<T>(-v.x, -v.y);
+  if (r == c) v = pf::cadd(v, z[b]);
+  dst[(size_t)b * stride + r + (size_t)c * ld] = v;
+}
+// dst_b = op(src) with src shared (stride 0) or per point; conj_t: conjugate transpose
+template <typename T>
+__global__ void k_copy(cx<T>* dst, long long sd, const cx<T>* src, long long ss, int lds, int rows, int cols,
+                       int ldd, int conj_t) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows * cols) return;
+  const int r = i % rows, c = i / rows;
+  const cx<T> v =
+      conj_t ? pf::cconj(src[(size_t)b * ss + c + (size_t)r * lds]) : src[(size_t)b * ss + r + (size_t)c * lds];
+  dst[(size_t)b * sd + r + (size_t)c * ldd] = v;
+}
+template <typename T>
+__global__ void k_add2(cx<T>* a, cx<T>* b2, const cx<T>* t, long long stride, int m, int ld, const int* active) {
+  const int b = blockIdx.y;
+  if (active && !active[b]) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m * m) return;
+  const size_t o = (size_t)b * stride + (i % m) + (size_t)(i / m) * ld;
+  a[o] = pf::cadd(a[o], t[o]);
+  b2[o] = pf::cadd(b2[o], t[o]);
+}
+template <typename T>
+__global__ void k_sub(cx<T>* a, const cx<T>* s, long long stride, int m, int ld) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m * m) return;
+  const size_t o = (size_t)b * stride + (i % m) + (size_t)(i / m) * ld;
+  a[o] = pf::csub(a[o], s[o]);
+}
+// G = sgn * i (S - S^H), sgn = +1 or -1
+template <typename T>
+__global__ void k_gamma(cx<T>* G, const cx<T>* S, long long stride, int m, int ld, int sgn) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m * m) return;
+  const int r = i % m, c = i / m;
+  const cx<T> a = S[(size_t)b * stride + r + (size_t)c * ld];
+  const cx<T> e = S[(size_t)b * stride + c + (size_t)r * ld];
+  const cx<T> d = pf::mk<T>(a.x - e.x, a.y + e.y);  // a - conj(e)
+  G[(size_t)b * stride + r + (size_t)c * ld] = sgn > 0 ? pf::mk<T>(-d.y, d.x) : pf::mk<T>(d.y, -d.x);
+}
+// per-point energies: zl = E - i eps, zr = E + i eps, zd = E + i dev eps
+template <typename T>
+__global__ void k_points(const double* E, const int* idx, int cnt, double eta, double eta0, double devf,
+                         cx<T>* zl, cx<T>* zr, cx<T>* zd, int* st) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= cnt) return;
+  const double e = E[idx[b]];
+  const double eps = e * eta + eta0;
+  zl[b] = pf::mk<T>(T(e), T(-eps));
+  zr[b] = pf::mk<T>(T(e), T(eps));
+  zd[b] = pf::mk<T>(T(e), T(devf * eps));
+  st[b] = 0;
+}
+__global__ void k_fill(int* a, int n, int v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = v;
+}
+__global__ void k_iota(int* a, int n, int start) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = start + i;
+}
+// decimation control: maxdiff of alpha per point, retire converged points
+template <typename T>
+__global__ void k_converge(const cx<T>* al, long long stride, int m, int ld, double conv, int max_iter, int* active,
+                           int* it, int* st, int* count, int first) {
+  const int b = blockIdx.x;
+  if (!active[b]) return;
+  double v = 0.0;
+  for (int i = threadIdx.x; i < m * m; i += blockDim.x) {
+    const cx<T> e = al[(size_t)b * stride + (i % m) + (size_t)(i / m) * ld];
+    const double h = hypot((double)e.x, (double)e.y);
+    v = (h > v || h != h) ? h : v;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    const double w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = (w > v || w != w) ? w : v;
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    v = red[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = (red[w] > v || red[w] != red[w]) ? red[w] : v;
+    if (!first) it[b] += 1;
+    if (v != v) {
+      st[b] |= pf::PF_NAN;
+      active[b] = 0;
+    } else if (!(v > conv)) {
+      active[b] = 0;
+    } else if (it[b] >= max_iter) {
+      st[b] |= pf::PF_NOT_CONVERGED;
+      active[b] = 0;
+    } else {
+      atomicAdd(count, 1);
+    }
+  }
+}
+// T = Re Tr(P Q), P (m x k), Q (k x m); scatter to the point's slot
+template <typename T>
+__global__ void k_trace(const cx<T>* P, const cx<T>* Q, long long stride, int m, int k, int ld, const int* idx,
+                        const int* zero_flag, const int* st, const int* itl, const int* itr, double* transl,
+                        int* status, int* iters) {
+  const int b = blockIdx.x;
+  double v = 0.0;
+  for (int i = threadIdx.x; i < m * k; i += blockDim.x) {
+    const int r = i % m, c = i / m;
+    const cx<T> a = P[(size_t)b * stride + r + (size_t)c * ld];
+    const cx<T> q = Q[(size_t)b * stride + c + (size_t)r * ld];
+    v += (double)a.x * (double)q.x - (double)a.y * (double)q.y;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w];
+    const int p = idx[b];
+    const bool zero = zero_flag && zero_flag[p];
+    transl[p] = (zero || v < 1.0e-60) ? 0.0 : v;
+    status[p] = st[b];
+    if (iters) {
+      iters[2 * p] = itl[b];
+      iters[2 * p + 1] = itr[b];
+    }
+  }
+}
+__global__ void k_mirror(const double* HL, const double* HLv, const double* HR, const double* HRv, size_t m2,
+                         int* diff) {
+  int d = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < m2; i += (size_t)gridDim.x * blockDim.x)
+    d |= (__double_as_longlong(HL[i]) != __double_as_longlong(HR[i])) |
+         (__double_as_longlong(HLv[i]) != __double_as_longlong(HRv[i]));
+  if (d) atomicOr(diff, 1);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct TLayout {
+  int n, nl, nr, m, nb, batch;
+  size_t mat;  // elements per working matrix (m * m, ld m)
+};
+
+size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+TLayout tlayout(int n, int nl, int nr, int npts, size_t cxb) {
+  TLayout l;
+  l.n = n;
+  l.nl = nl;
+  l.nr = nr;
+  l.m = std::max(n, std::max(nl, nr));
+  l.mat = (size_t)l.m * l.m;
+  int nb = 32;
+  while (nb > 4 && ((size_t)l.m * nb + l.m) * cxb > kPanelBytes) nb >>= 1;
+  l.nb = nb;
+  const size_t per_point = (kMats * l.mat + 2 * (size_t)l.m * nb + (size_t)nb * nb + 8) * cxb + (size_t)l.m * 4 + 64;
+  size_t b = kBatchBytes / per_point;
+  if (b < 1) b = 1;
+  if (b > (size_t)kMaxBatch) b = kMaxBatch;
+  if (npts > 0 && (size_t)npts < b) b = npts;
+  l.batch = (int)b;
+  return l;
+}
+
+template <typename T>
+struct Work {
+  cx<T>* mats[kMats];  // each [batch] matrices of mat elements
+  cx<T>* P;
+  cx<T>* W;
+  cx<T>* M11;
+  cx<T>* zl;
+  cx<T>* zr;
+  cx<T>* zd;
+  int* piv;
+  int* idx;
+  int* active;
+  int* itl;
+  int* itr;
+  int* st;
+  int* counter;
+};
+
+// Carves the workspace (base == nullptr: only counts the bytes).
+template <typename T>
+size_t carve(char* base, const TLayout& L, Work<T>* w) {
+  const size_t cxb = sizeof(cx<T>);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* r = base ? base + off : nullptr;
+    off += round256(bytes);
+    return r;
+  };
+  const size_t B = (size_t)L.batch;
+  w->counter = reinterpret_cast<int*>(take(256));
+  w->idx = reinterpret_cast<int*>(take(B * 4));
+  w->active = reinterpret_cast<int*>(take(B * 4));
+  w->itl = reinterpret_cast<int*>(take(B * 4));
+  w->itr = reinterpret_cast<int*>(take(B * 4));
+  w->st = reinterpret_cast<int*>(take(B * 4));
+  w->zl = reinterpret_cast<cx<T>*>(take(B * cxb));
+  w->zr = reinterpret_cast<cx<T>*>(take(B * cxb));
+  w->zd = reinterpret_cast<cx<T>*>(take(B * cxb));
+  w->piv = reinterpret_cast<int*>(take(B * L.m * 4));
+  for (int i = 0; i < kMats; ++i) w->mats[i] = reinterpret_cast<cx<T>*>(take(B * L.mat * cxb));
+  w->P = reinterpret_cast<cx<T>*>(take(B * L.m * L.nb * cxb));
+  w->W = reinterpret_cast<cx<T>*>(take(B * L.m * L.nb * cxb));
+  w->M11 = reinterpret_cast<cx<T>*>(take(B * L.nb * L.nb * cxb));
+  return off;
+}
+
+template <typename T>
+struct Engine {
+  cudaStream_t s;
+  int B;  // points in flight
+  TLayout L;
+  Work<T> w;
+  int* host_count;
+
+  dim3 eg(int elems) const { return dim3((elems + 255) / 256, B); }
+
+  cudaError_t gemm(int m, int n, int k, const cx<T>* A, int lda, long long sA, bool ca, const cx<T>* Bm, int ldb,
+                   long long sB, bool cb, cx<T>* C, int ldc, long long sC, cx<T> alpha, cx<T> beta,
+                   const int* active, const cx<T>* zdiag = nullptr, const cx<T>* H = nullptr, int ldh = 0,
+                   long long sH = 0) {
+    if (m <= 0 || n <= 0) return cudaSuccess;
+    GemmArgs<T> g;
+    g.m = m;
+    g.n = n;
+    g.k = k;
+    g.A = A;
+    g.lda = lda;
+    g.sA = sA;
+    g.B = Bm;
+    g.ldb = ldb;
+    g.sB = sB;
+    g.C = C;
+    g.ldc = ldc;
+    g.sC = sC;
+    g.alpha = alpha;
+    g.beta = beta;
+    g.active = active;
+    g.zdiag = zdiag;
+    g.H = H;
+    g.ldh = ldh;
+    g.sH = sH;
+    const dim3 grid((m + BM - 1) / BM, (n + BN - 1) / BN, B);
+    if (!ca && !cb)
+      bgemm<T, false, false><<<grid, GT, 0, s>>>(g);
+    else if (ca && !cb)
+      bgemm<T, true, false><<<grid, GT, 0, s>>>(g);
+    else if (!ca && cb)
+      bgemm<T, false, true><<<grid, GT, 0, s>>>(g);
+    else
+      bgemm<T, true, true><<<grid, GT, 0, s>>>(g);
+    return cudaGetLastError();
+  }
+
+  // In-place inverse of the n x n leading block of every matrix of A.
+  int inverse(cx<T>* A, int n, const int* active) {
+    const int ld = L.m;
+    const long long sA = (long long)L.mat;
+    const size_t small = ((size_t)(n | 1) * n + 2 * (size_t)n) * sizeof(cx<T>) + ((size_t)n + 1) * 4;
+    if (small <= kSmallInvBytes) {
+      TL_CUDA(cudaFuncSetAttribute(inv_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small));
+      inv_small<T><<<B, 256, small, s>>>(A, ld, sA, n, active, w.st);
+      TL_CUDA(cudaGetLastError());
+      return PF_SUCCESS;
+    }
+    const int nb = L.nb;
+    const size_t psm = ((size_t)n * nb + n) * sizeof(cx<T>);
+    TL_CUDA(cudaFuncSetAttribute(gje_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm));
+    const cx<T> one = hmk<T>(T(1), T(0)), zero = hmk<T>(T(0), T(0));
+    for (int k = 0; k < n; k += nb) {
+      const int kb = std::min(nb, n - k);
+      gje_panel<T><<<B, 256, psm, s>>>(A, ld, sA, n, k, kb, w.piv, w.P, w.M11, active, w.st);
+      gje_swap<T><<<dim3((n + 255) / 256, B), 256, 0, s>>>(A, ld, sA, n, k, kb, w.piv, w.W, active);
+      const long long sP = (long long)n * kb, sW = (long long)kb * n, sM = (long long)kb * kb;
+      // rows above and below the pivot rows: += (factored panel rows) W
+      TL_CUDA(gemm(k, n, kb, w.P, n, sP, false, w.W, kb, sW, false, A, ld, sA, one, one, active));
+      TL_CUDA(gemm(n - k - kb, n, kb, w.P + (k + kb), n, sP, false, w.W, kb, sW, false, A + (k + kb), ld, sA, one,
+                   one, active));
+      // pivot rows: = M11 W
+      TL_CUDA(gemm(kb, n, kb, w.M11, kb, sM, false, w.W, kb, sW, false, A + k, ld, sA, one, zero, active));
+      gje_restore<T><<<dim3((n * kb + 255) / 256, B), 256, 0, s>>>(A, ld, sA, n, k, kb, w.P, active);
+    }
+    gje_unpermute<T><<<B, 256, 0, s>>>(A, ld, sA, n, w.piv, active);
+    TL_CUDA(cudaGetLastError());
+    return PF_SUCCESS;
+  }
+
+  // Lopez-Sancho decimation of one lead for the batch (surface.f90:479-497)
+  // with alpha0 = v^H, beta0 = v; g = inv(z - es) into out.
+  int decimate(int m, const cx<T>* h00, const cx<T>* v, const cx<T>* z, double conv, int max_iter, int* it,
+               cx<T>* out) {
+    const int ld = L.m;
+    const long long sm = (long long)L.mat;
+    cx<T>* al = w.mats[0];
+    cx<T>* be = w.mats[1];
+    cx<T>* e1 = w.mats[2];
+    cx<T>* es = w.mats[3];
+    cx<T>* W1 = w.mats[4];
+    cx<T>* A2 = w.mats[5];
+    cx<T>* B2 = w.mats[6];
+    cx<T>* TT = w.mats[7];
+    cx<T>* aln = w.mats[8];
+    cx<T>* ben = w.mats[9];
+    const cx<T> one = hmk<T>(T(1), T(0)), zero = hmk<T>(T(0), T(0));
+    k_copy<T><<<eg(m * m), 256, 0, s>>>(e1, sm, h00, 0, m, m, m, ld, 0);
+    k_copy<T><<<eg(m * m), 256, 0, s>>>(es, sm, h00, 0, m, m, m, ld, 0);
+    k_copy<T><<<eg(m * m), 256, 0, s>>>(al, sm, v, 0, m, m, m, ld, 1);
+    k_copy<T><<<eg(m * m), 256, 0, s>>>(be, sm, v, 0, m, m, m, ld, 0);
+    k_fill<<<(B + 255) / 256, 256, 0, s>>>(it, B, 0);
+    k_fill<<<(B + 255) / 256, 256, 0, s>>>(w.active, B, 1);
+    TL_CUDA(cudaGetLastError());
+    int first = 1;
+    for (;;) {
+      k_fill<<<1, 32, 0, s>>>(w.counter, 1, 0);
+      k_converge<T><<<B, 256, 0, s>>>(al, sm, m, ld, conv, max_iter, w.active, it, w.st, w.counter, first);
+      first = 0;
+      TL_CUDA(cudaGetLastError());
+      TL_CUDA(cudaStreamSynchronize(s));
+      TL_CUDA(cudaMemcpy(host_count, w.counter, sizeof(int), cudaMemcpyDeviceToHost));
+      if (*host_count == 0) break;
+      k_shift_neg<T><<<eg(m * m), 256, 0, s>>>(W1, e1, sm, m, ld, z, w.active);
+      int rc = inverse(W1, m, w.active);
+      if (rc) return rc;
+      TL_CUDA(gemm(m, m, m, al, ld, sm, false, W1, ld, sm, false, A2, ld, sm, one, zero, w.active));
+      TL_CUDA(gemm(m, m, m, be, ld, sm, false, W1, ld, sm, false, B2, ld, sm, one, zero, w.active));
+      TL_CUDA(gemm(m, m, m, A2, ld, sm, false, be, ld, sm, false, TT, ld, sm, one, zero, w.active));
+      k_add2<T><<<eg(m * m), 256, 0, s>>>(e1, es, TT, sm, m, ld, w.active);
+      TL_CUDA(gemm(m, m, m, B2, ld, sm, false, al, ld, sm, false, e1, ld, sm, one, one, w.active));
+      TL_CUDA(gemm(m, m, m, A2, ld, sm, false, al, ld, sm, false, aln, ld, sm, one, zero, w.active));
+      TL_CUDA(gemm(m, m, m, B2, ld, sm, false, be, ld, sm, false, ben, ld, sm, one, zero, w.active));
+      std::swap(al, aln);
+      std::swap(be, ben);
+    }
+    k_shift_neg<T><<<eg(m * m), 256, 0, s>>>(out, es, sm, m, ld, z, nullptr);
+    TL_CUDA(cudaGetLastError());
+    return inverse(out, m, nullptr);
+  }
+
+  // One batch of points sharing block set q: leads, sweep, Caroli.
+  int run(const pf::System<double>& sys, int q, const double* E, int cnt, double eta, double eta0, double devf,
+          double conv, int max_iter, bool mirror, const int* zero_flag, double* transl, int* status, int* iters) {
+    const int n = L.n, nl = L.nl, nr = L.nr, Ld = sys.L, ld = L.m;
+    const long long sm = (long long)L.mat;
+    const cx<T> one = hmk<T>(T(1), T(0)), zero = hmk<T>(T(0), T(0)), mone = hmk<T>(T(-1), T(0));
+    const cx<T>* HL = reinterpret_cast<const cx<T>*>(sys.HL) + (size_t)q * nl * nl;
+    const cx<T>* HLv = reinterpret_cast<const cx<T>*>(sys.HLv) + (size_t)q * nl * nl;
+    const cx<T>* HR = reinterpret_cast<const cx<T>*>(sys.HR) + (size_t)q * nr * nr;
+    const cx<T>* HRv = reinterpret_cast<const cx<T>*>(sys.HRv) + (size_t)q * nr * nr;
+    const cx<T>* Hd = reinterpret_cast<const cx<T>*>(sys.Hd) + (size_t)q * Ld * n * n;
+    const cx<T>* Hdv = reinterpret_cast<const cx<T>*>(sys.Hdv) + (size_t)q * (Ld > 1 ? Ld - 1 : 0) * n * n;
+    const cx<T>* Hld = reinterpret_cast<const cx<T>*>(sys.Hld) + (size_t)q * nl * n;
+    const cx<T>* Hrd = reinterpret_cast<const cx<T>*>(sys.Hrd) + (size_t)q * nr * n;
+    k_points<T><<<(cnt + 127) / 128, 128, 0, s>>>(E, w.idx, cnt, eta, eta0, devf, w.zl, w.zr, w.zd, w.st);
+    TL_CUDA(cudaGetLastError());
+    cx<T>* gl = w.mats[10];
+    cx<T>* sl = w.mats[11];
+    cx<T>* gml = w.mats[12];
+    cx<T>* gr = w.mats[13];
+    cx<T>* sr = w.mats[14];
+    cx<T>* gmr = w.mats[15];
+    cx<T>* t0 = w.mats[0];
+    cx<T>* t1 = w.mats[1];
+    cx<T>* t2 = w.mats[2];
+    int rc;
+    // ---- left lead, advanced: z = E - i eps, alpha0 = Hlv^H, beta0 = Hlv
+    if ((rc = decimate(nl, HL, HLv, w.zl, conv, max_iter, w.itl, t1))) return rc;
+    TL_CUDA(gemm(nl, nl, nl, t1, ld, sm, false, HLv, nl, 0, false, t0, ld, sm, one, zero, nullptr));  // g V
+    TL_CUDA(gemm(nl, nl, nl, HLv, nl, 0, true, t0, ld, sm, false, t2, ld, sm, one, zero, nullptr));   // sl_adv
+    // wrapper conversions (lesser.f90:141-144): gl = gl_adv^H, sl = sl_adv^H, gml = -gml_adv
+    k_copy<T><<<eg(nl * nl), 256, 0, s>>>(gl, sm, t1, sm, ld, nl, nl, ld, 1);
+    k_copy<T><<<eg(nl * nl), 256, 0, s>>>(sl, sm, t2, sm, ld, nl, nl, ld, 1);
+    k_gamma<T><<<eg(nl * nl), 256, 0, s>>>(gml, t2, sm, nl, ld, -1);
+    TL_CUDA(cudaGetLastError());
+    // ---- right lead, retarded: z = E + i eps
+    if (mirror) {
+      // identical leads: gr_ret = gl_adv^H, sr_ret = sl_adv^H, gmr_ret = -gml_adv
+      k_copy<T><<<eg(nr * nr), 256, 0, s>>>(gr, sm, gl, sm, ld, nr, nr, ld, 0);
+      k_copy<T><<<eg(nr * nr), 256, 0, s>>>(sr, sm, sl, sm, ld, nr, nr, ld, 0);
+      k_copy<T><<<eg(nr * nr), 256, 0, s>>>(gmr, sm, gml, sm, ld, nr, nr, ld, 0);
+      TL_CUDA(cudaMemcpyAsync(w.itr, w.itl, sizeof(int) * B, cudaMemcpyDeviceToDevice, s));
+    } else {
+      if ((rc = decimate(nr, HR, HRv, w.zr, conv, max_iter, w.itr, gr))) return rc;
+      TL_CUDA(gemm(nr, nr, nr, gr, ld, sm, false, HRv, nr, 0, false, t0, ld, sm, one, zero, nullptr));
+      TL_CUDA(gemm(nr, nr, nr, HRv, nr, 0, true, t0, ld, sm, false, sr, ld, sm, one, zero, nullptr));
+      k_gamma<T><<<eg(nr * nr), 256, 0, s>>>(gmr, sr, sm, nr, ld, 1);
+    }
+    TL_CUDA(cudaGetLastError());
+    // ---- left-to-right sweep (lesser.f90:547-654)
+    cx<T>* g = w.mats[0];
+    cx<T>* A = w.mats[1];
+    cx<T>* T1 = w.mats[2];
+    cx<T>* G0N = w.mats[3];
+    cx<T>* U = w.mats[4];
+    // layer 1: T1 = gl Hld (nl x n); g = inv(zD - Hd_1 - Hld^H T1); G0N = T1 g
+    TL_CUDA(gemm(nl, n, nl, gl, ld, sm, false, Hld, nl, 0, false, T1, ld, sm, one, zero, nullptr));
+    TL_CUDA(gemm(n, n, nl, Hld, nl, 0, true, T1, ld, sm, false, g, ld, sm, mone, zero, nullptr, w.zd, Hd, n, 0));
+    if ((rc = inverse(g, n, nullptr))) return rc;
+    TL_CUDA(gemm(nl, n, n, T1, ld, sm, false, g, ld, sm, false, G0N, ld, sm, one, zero, nullptr));
+    for (int i = 1; i < Ld; ++i) {
+      const cx<T>* V = Hdv + (size_t)(i - 1) * n * n;
+      TL_CUDA(gemm(n, n, n, g, ld, sm, false, V, n, 0, false, T1, ld, sm, one, zero, nullptr));
+      TL_CUDA(gemm(n, n, n, V, n, 0, true, T1, ld, sm, false, A, ld, sm, mone, zero, nullptr, w.zd,
+                   Hd + (size_t)i * n * n, n, 0));
+      if ((rc = inverse(A, n, nullptr))) return rc;
+      TL_CUDA(gemm(nl, n, n, G0N, ld, sm, false, V, n, 0, false, U, ld, sm, one, zero, nullptr));
+      TL_CUDA(gemm(nl, n, n, U, ld, sm, false, A, ld, sm, false, G0N, ld, sm, one, zero, nullptr));
+      std::swap(g, A);
+    }
+    // right closure: A = inv(zD - HR - sr - Hrd g Hrd^H); G_{0,N+1} = G0N Hrd^H A
+    TL_CUDA(gemm(n, nr, n, g, ld, sm, false, Hrd, nr, 0, true, T1, ld, sm, one, zero, nullptr));
+    TL_CUDA(gemm(nr, nr, n, Hrd, nr, 0, false, T1, ld, sm, false, A, ld, sm, mone, zero, nullptr, w.zd, HR, nr, 0));
+    k_sub<T><<<eg(nr * nr), 256, 0, s>>>(A, sr, sm, nr, ld);
+    if ((rc = inverse(A, nr, nullptr))) return rc;
+    TL_CUDA(gemm(nl, nr, n, G0N, ld, sm, false, Hrd, nr, 0, true, U, ld, sm, one, zero, nullptr));
+    TL_CUDA(gemm(nl, nr, nr, U, ld, sm, false, A, ld, sm, false, T1, ld, sm, one, zero, nullptr));  // G_D_LR
+    // Caroli: Re Tr[(G gmr)(G^H gml)]
+    TL_CUDA(gemm(nl, nr, nr, T1, ld, sm, false, gmr, ld, sm, false, U, ld, sm, one, zero, nullptr));
+    TL_CUDA(gemm(nr, nl, nl, T1, ld, sm, true, gml, ld, sm, false, g, ld, sm, one, zero, nullptr));
+    k_trace<T><<<cnt, 256, 0, s>>>(U, g, sm, nl, nr, ld, w.idx, zero_flag, w.st, w.itl, w.itr, transl, status,
+                                   iters);
+    TL_CUDA(cudaGetLastError());
+    return PF_SUCCESS;
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* pf_tiled_last_error(void) { return g_err; }
+
+size_t pf_transport_tdb_tiled_workspace_size(int n, int nl, int nr, int nq, int npts) {
+  if (n <= 0 || nl <= 0 || nr <= 0 || nq <= 0 || npts < 0) return 0;
+  if (n > PF_NMAX_TILED || nl > PF_NMAX_TILED || nr > PF_NMAX_TILED) return 0;
+  const TLayout L = tlayout(n, nl, nr, npts, sizeof(cx<double>));
+  Work<double> w;
+  return 256 + carve<double>(nullptr, L, &w);
+}
+
+int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
+                               const double* HR, const double* HRv, const double* Hd, const double* Hdv,
+                               const double* Hld, const double* Hrd, int npts, const double* E, const int* qidx,
+                               const int* zero_flag, double eta, double eta0, double dev_factor, double convergence,
+                               int max_iter, double* transl, int* status, int* iters, void* work,
+                               size_t work_bytes, void* stream) {
+  if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0)
+    return set_err(PF_ERR_ARG, "pf_tiled: dimensions must be positive");
+  if (n > PF_NMAX_TILED || nl > PF_NMAX_TILED || nr > PF_NMAX_TILED)
+    return set_err(PF_ERR_SIZE, "pf_tiled: block size exceeds PF_NMAX_TILED");
+  if (!HL || !HLv || !HR || !HRv || !Hd || !Hld || !Hrd || (L > 1 && !Hdv))
+    return set_err(PF_ERR_ARG, "pf_tiled: null block pointer");
+  if (!E || !transl || !status) return set_err(PF_ERR_ARG, "pf_tiled: null pointer");
+  if (max_iter <= 0) return set_err(PF_ERR_ARG, "pf_tiled: max_iter must be positive");
+  if (npts == 0) return PF_SUCCESS;
+  Engine<double> e;
+  e.L = tlayout(n, nl, nr, npts, sizeof(cx<double>));
+  const size_t need = 256 + carve<double>(nullptr, e.L, &e.w);
+  if (!work || work_bytes < need) return set_err(PF_ERR_ARG, "pf_tiled: workspace too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  char* base = reinterpret_cast<char*>(work);
+  int* mirror_dev = reinterpret_cast<int*>(base);  // 256-byte header
+  carve<double>(base + 256, e.L, &e.w);
+  e.s = st;
+  int host_count = 0;
+  e.host_count = &host_count;
+  // group the points by q (host copy of qidx)
+  std::vector<int> q(npts, 0);
+  if (qidx) {
+    TL_CUDA(cudaStreamSynchronize(st));
+    TL_CUDA(cudaMemcpy(q.data(), qidx, sizeof(int) * npts, cudaMemcpyDeviceToHost));
+  }
+  for (int i = 0; i < npts; ++i)
+    if (q[i] < 0 || q[i] >= nq) return set_err(PF_ERR_ARG, "pf_tiled: qidx out of range");
+  std::vector<int> order(npts);
+  for (int i = 0; i < npts; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return q[a] < q[b]; });
+  pf::System<double> sys;
+  sys.n = n;
+  sys.nl = nl;
+  sys.nr = nr;
+  sys.L = L;
+  sys.nq = nq;
+  sys.HL = reinterpret_cast<const cx<double>*>(HL);
+  sys.HLv = reinterpret_cast<const cx<double>*>(HLv);
+  sys.HR = reinterpret_cast<const cx<double>*>(HR);
+  sys.HRv = reinterpret_cast<const cx<double>*>(HRv);
+  sys.Hd = reinterpret_cast<const cx<double>*>(Hd);
+  sys.Hdv = reinterpret_cast<const cx<double>*>(Hdv);
+  sys.Hld = reinterpret_cast<const cx<double>*>(Hld);
+  sys.Hrd = reinterpret_cast<const cx<double>*>(Hrd);
+  size_t i0 = 0;
+  while (i0 < (size_t)npts) {
+    const int qq = q[order[i0]];
+    size_t i1 = i0;
+    while (i1 < (size_t)npts && q[order[i1]] == qq) ++i1;
+    bool mirror = false;
+    if (nl == nr) {
+      k_fill<<<1, 32, 0, st>>>(mirror_dev, 1, 0);
+      const size_t off = (size_t)qq * nl * nl * 2;
+      k_mirror<<<64, 256, 0, st>>>(HL + off, HLv + off, HR + off, HRv + off, (size_t)nl * nl * 2, mirror_dev);
+      TL_CUDA(cudaGetLastError());
+      TL_CUDA(cudaStreamSynchronize(st));
+      int diff = 1;
+      TL_CUDA(cudaMemcpy(&diff, mirror_dev, sizeof(int), cudaMemcpyDeviceToHost));
+      mirror = (diff == 0);
+    }
+    for (size_t c0 = i0; c0 < i1; c0 += (size_t)e.L.batch) {
+      const int cnt = (int)std::min((size_t)e.L.batch, i1 - c0);
+      if (!qidx) {
+        k_iota<<<(cnt + 255) / 256, 256, 0, st>>>(e.w.idx, cnt, (int)c0);
+        TL_CUDA(cudaGetLastError());
+      } else {
+        TL_CUDA(cudaStreamSynchronize(st));
+        TL_CUDA(cudaMemcpy(e.w.idx, order.data() + c0, sizeof(int) * cnt, cudaMemcpyHostToDevice));
+      }
+      e.B = cnt;
+      const int rc = e.run(sys, qq, E, cnt, eta, eta0, dev_factor, convergence, max_iter, mirror, zero_flag, transl,
+                           status, iters);
+      if (rc) return rc;
+    }
+    i0 = i1;
+  }
+  TL_CUDA(cudaStreamSynchronize(st));
+  return PF_SUCCESS;
+}
+
+}  // extern "C"

@@ -80,6 +80,47 @@ def _ptr(a, ctype=C.c_double):
     return a.ctypes.data_as(C.POINTER(ctype))
 
 
+NMAX_RESIDENT = 48   # PF_NMAX_RESIDENT
+
+
+def _transport_tiled(E, nq, dims, arrs, *, eta, eta0, convergence, dev_factor, qidx, zero_flag, max_iter,
+                     want_transr, check, precision):
+    """Blocks above the resident size: pf_transport_tdb_tiled_dev on torch
+    device buffers (T_L only, FP64)."""
+    import torch
+    if want_transr:
+        raise ValueError("T_R is not computed for blocks above 48 (pass want_transr=False)")
+    if precision != "fp64":
+        raise ValueError("blocks above 48 run in FP64 (precision='fp64')")
+    lib = _abi.load()
+    n, nl, nr, L = dims
+    dev = {k: torch.from_numpy(fortran_block(v).copy()).cuda() for k, v in arrs.items()}
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    npts = E.size
+    Ed = torch.from_numpy(E).cuda()
+    qd = None if qidx is None else torch.from_numpy(np.ascontiguousarray(qidx, dtype=np.int32)).cuda()
+    zd = None if zero_flag is None else torch.from_numpy(np.ascontiguousarray(zero_flag, dtype=np.int32)).cuda()
+    tl = torch.zeros(max(npts, 1), dtype=torch.float64, device="cuda")
+    st = torch.zeros(max(npts, 1), dtype=torch.int32, device="cuda")
+    it = torch.zeros((max(npts, 1), 2), dtype=torch.int32, device="cuda")
+    ws = lib.pf_transport_tdb_tiled_workspace_size(n, nl, nr, nq, npts)
+    if ws == 0:
+        _abi.check(-3)
+    work = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    p = lambda t: None if t is None else t.data_ptr()
+    rc = lib.pf_transport_tdb_tiled_dev(n, nl, nr, L, nq, *[dev[k].data_ptr() for k in BLOCK_NAMES], npts,
+                                        Ed.data_ptr(), p(qd), p(zd), eta, eta0, dev_factor, convergence, max_iter,
+                                        tl.data_ptr(), st.data_ptr(), it.data_ptr(), work.data_ptr(), ws,
+                                        C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if rc != 0:
+        raise _abi.PFError(rc, lib.pf_tiled_last_error().decode(errors="replace"))
+    torch.cuda.synchronize()
+    status = st.cpu().numpy()[:npts]
+    if check and (status != 0).any():
+        raise _abi.PFError(-4, f"point status flags 0x{int(np.bitwise_or.reduce(status)):x}")
+    return dict(transl=tl.cpu().numpy()[:npts], transr=None, status=status, iters=it.cpu().numpy()[:npts])
+
+
 def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=None,
                   zero_flag=None, max_iter=1000, want_transr=True, check=True,
                   precision="fp64", refine_iters=1):
@@ -99,6 +140,10 @@ def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=No
     if isinstance(blocks, dict):
         blocks = TdbBlocks.from_dict(blocks)
     nq, (n, nl, nr, L), arrs = blocks.stacked()
+    if max(n, nl, nr) > NMAX_RESIDENT:
+        return _transport_tiled(E, nq, (n, nl, nr, L), arrs, eta=eta, eta0=eta0, convergence=convergence,
+                                dev_factor=dev_factor, qidx=qidx, zero_flag=zero_flag, max_iter=max_iter,
+                                want_transr=want_transr, check=check, precision=precision)
     buf = {k: fortran_block(v) for k, v in arrs.items()}
     E = np.ascontiguousarray(E, dtype=np.float64)
     npts = E.shape[0]

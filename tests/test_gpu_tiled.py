@@ -1,0 +1,61 @@
+"""Large-block FP64 path (pf_transport_tdb_tiled_dev) against the oracle:
+blocks above the resident limit (48), both the shared-memory inverse and the
+blocked Gauss-Jordan inverse (ragged last panel), several q block sets."""
+import numpy as np
+import pytest
+
+from oracle import negf as N
+from phinfortran_gb300 import systems as S
+from phinfortran_gb300 import transport_tdb
+
+pytestmark = pytest.mark.gpu
+
+
+def check_against_oracle(b, E, p, qidx=None, zf=None, tol=1e-9):
+    r = transport_tdb(E, b, want_transr=False, qidx=qidx, zero_flag=zf, **p)
+    assert (r["status"] == 0).all()
+    if qidx is None:
+        o = N.transport(E, b, p["eta"], p["eta0"], p["convergence"], p["dev_factor"],
+                        zero_first=None if zf is None else zf.astype(bool))
+        To, it = o["transl"], o["iters_left"]
+    else:
+        To = np.zeros(E.size)
+        it = np.zeros(E.size, dtype=int)
+        for q in np.unique(qidx):
+            sel = qidx == q
+            bq = {k: v[q] for k, v in b.items()}
+            o = N.transport(E[sel], bq, p["eta"], p["eta0"], p["convergence"], p["dev_factor"])
+            To[sel] = o["transl"]
+            it[sel] = o["iters_left"]
+    err = np.abs(r["transl"] - To) / np.maximum(np.abs(To), 1.0)
+    assert err.max() < tol, (err.max(), np.argmax(err))
+    # same stopping rule as the oracle's decimation
+    assert np.abs(r["iters"][:, 0] - it).max() <= 1
+    return r, To
+
+
+def test_tiled_small_inverse(cuda_ready):
+    """6 x 6 cross-section: n = 108 (shared-memory inverse)."""
+    b, E, p, _ = S.sc_phonon(nx=6, ny=6, L=5, ne=20, seed_index=11)
+    zf = np.zeros(E.size, np.int32)
+    zf[0] = 1
+    r, o = check_against_oracle(b, E, p, zf=zf)
+    assert r["transl"][0] == 0.0
+    assert o.max() > 1.0
+
+
+def test_tiled_blocked_inverse(cuda_ready):
+    """7 x 7 cross-section: n = 147 -> blocked Gauss-Jordan, panels of 32
+    and a last panel of 19 columns."""
+    b, E, p, _ = S.sc_phonon(nx=7, ny=7, L=3, ne=10, seed_index=12)
+    check_against_oracle(b, E[1:], p)
+
+
+def test_tiled_multi_q(cuda_ready):
+    """Two block sets (different disorder seeds) interleaved in one call."""
+    b1, E, p, _ = S.sc_phonon(nx=6, ny=6, L=4, ne=12, seed_index=13)
+    b2, _, _, _ = S.sc_phonon(nx=6, ny=6, L=4, ne=12, seed_index=14)
+    st = {k: np.stack([b1[k], b2[k]]) for k in b1}
+    Eint = np.repeat(E[1:], 2)
+    q = np.tile(np.array([0, 1], dtype=np.int32), E.size - 1)
+    check_against_oracle(st, Eint, p, qidx=q)
