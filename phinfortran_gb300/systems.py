@@ -170,3 +170,91 @@ def sc_phonon(nx=4, ny=4, L=20, k=1.0, mass_range=(1.0, 2.0), lead_mass=1.0, ne=
     params = dict(eta=0.0, eta0=eta, dev_factor=10.0, convergence=convergence)
     aux = dict(bar=bar, masses=masses, springs=springs, omega=w, omega_max=wmax)
     return blocks, E, params, aux
+
+
+def _diamond_layer(nc, a=1.0):
+    """Atom positions of one layer: nc x nc conventional diamond cells,
+    one cell thick along z (8 nc^2 atoms)."""
+    fcc = np.array([[0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0]], dtype=np.float64)
+    basis = np.concatenate([fcc, fcc + 0.25])
+    pos = [basis + np.array([ix, iy, 0.0]) for ix in range(nc) for iy in range(nc)]
+    return np.concatenate(pos) * a
+
+
+def _diamond_force_blocks(nc, kgrid, k1, k2, a=1.0, tol=1e-6):
+    """Onsite (layer j, j) and coupling (layer j, j+1) force-constant blocks
+    of a periodic nc x nc diamond slab with central first- and second-
+    neighbour springs, Bloch-summed over the transverse images for every k
+    (fractional units of the slab's transverse reciprocal vectors)."""
+    pos = _diamond_layer(nc, a)
+    na = pos.shape[0]
+    d1, d2 = a * np.sqrt(3) / 4, a / np.sqrt(2)
+    nk = kgrid.shape[0]
+    F0 = np.zeros((nk, 3 * na, 3 * na), np.complex128)
+    F1 = np.zeros((nk, 3 * na, 3 * na), np.complex128)
+    self_term = np.zeros((na, 3, 3))
+    for ix in (-1, 0, 1):
+        for iy in (-1, 0, 1):
+            for dz in (-1, 0, 1):
+                shift = np.array([ix * nc * a, iy * nc * a, dz * a])
+                r = pos[None, :, :] + shift - pos[:, None, :]          # (a, b, 3)
+                d = np.linalg.norm(r, axis=-1)
+                kk = np.where(np.abs(d - d1) < tol, k1, np.where(np.abs(d - d2) < tol, k2, 0.0))
+                ia, ib = np.nonzero(kk)
+                if ia.size == 0:
+                    continue
+                e = r[ia, ib] / d[ia, ib][:, None]
+                K = kk[ia, ib][:, None, None] * e[:, :, None] * e[:, None, :]   # (pairs, 3, 3)
+                np.add.at(self_term, ia, K)
+                if dz < 0:
+                    continue
+                ph = np.exp(2j * np.pi * (kgrid[:, 0] * ix + kgrid[:, 1] * iy))  # (nk,)
+                tgt = F0 if dz == 0 else F1
+                for p in range(ia.size):
+                    A, B = 3 * ia[p], 3 * ib[p]
+                    tgt[:, A:A + 3, B:B + 3] -= ph[:, None, None] * K[p][None]
+    for A in range(na):
+        F0[:, 3 * A:3 * A + 3, 3 * A:3 * A + 3] += self_term[A][None]
+    return F0, F1
+
+
+def diamond_phonon(nc=2, L=60, nk_side=8, ne=512, k1=1.0, k2=0.2, masses=(28.0, 72.6), block=10, eta=1e-5,
+                   convergence=1e-14, kpoints=None):
+    """Phonons of a diamond-lattice slab stack with a mass interface.
+
+    Cross-section nc x nc conventional cells (n = 24 nc^2 DOF per layer, one
+    cell thick), periodic transversally with Bloch wave vectors on an
+    nk_side x nk_side grid centred as the reference's transverse mesh
+    (negf/config.f90:153-175); central springs k1 (first neighbours) and k2
+    (second neighbours).  Device layers alternate masses[0] / masses[1] in
+    blocks of `block` layers; each lead takes the mass of the device block
+    next to it.  Frequencies uniform on (0, omega_max] with omega_max the top
+    of the left lead's spectrum; E = omega^2, eta = 0, eta0 = eta.
+    ``kpoints`` selects a subset of the grid (indices).  Returns the
+    q-stacked blocks, E, params and aux (kgrid, omega, n).
+    """
+    n1 = nk_side
+    g = np.array([[(i / n1) - 0.5 * (n1 - 1) / n1, (j / n1) - 0.5 * (n1 - 1) / n1, 0.0]
+                  for i in range(n1) for j in range(n1)])
+    if n1 == 1:
+        g[:] = 0.0
+    if kpoints is not None:
+        g = g[np.asarray(kpoints)]
+    F0, F1 = _diamond_force_blocks(nc, g, k1, k2)
+    n = F0.shape[-1]
+    layer_mass = np.array([masses[(j // block) % 2] for j in range(L)], dtype=np.float64)
+    mL, mR = layer_mass[0], layer_mass[-1]
+    s = 1.0 / np.sqrt(layer_mass)
+    Hd = F0[:, None] * (s ** 2)[None, :, None, None]
+    Hdv = F1[:, None] * (s[:-1] * s[1:])[None, :, None, None] if L > 1 else np.zeros((g.shape[0], 0, n, n))
+    blocks = dict(HL=F0 / mL, HLv=F1 / mL, HR=F0 / mR, HRv=np.conj(np.swapaxes(F1, -1, -2)) / mR,
+                  Hd=Hd, Hdv=Hdv, Hld=F1 / np.sqrt(mL * layer_mass[0]),
+                  Hrd=np.conj(np.swapaxes(F1, -1, -2)) / np.sqrt(layer_mass[-1] * mR))
+    # top of the left lead's band at k = 0 of the first transverse point
+    Hb = F0[0] + F1[0] + np.conj(F1[0].T)
+    Hpi = F0[0] - F1[0] - np.conj(F1[0].T)
+    wmax = np.sqrt(max(np.linalg.eigvalsh(Hb).max(), np.linalg.eigvalsh(Hpi).max()) / mL)
+    w = wmax * np.arange(1, ne + 1) / ne
+    params = dict(eta=0.0, eta0=eta, dev_factor=10.0, convergence=convergence)
+    aux = dict(kgrid=g, omega=w, omega_max=wmax, n=n, layer_mass=layer_mass)
+    return blocks, w ** 2, params, aux

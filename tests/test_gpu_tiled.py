@@ -59,3 +59,19 @@ def test_tiled_multi_q(cuda_ready):
     Eint = np.repeat(E[1:], 2)
     q = np.tile(np.array([0, 1], dtype=np.int32), E.size - 1)
     check_against_oracle(st, Eint, p, qidx=q)
+
+
+def test_tiled_diamond_slab_interface(cuda_ready):
+    """Diamond slab stack (2 x 2 conventional cells, n = 96) with a 28 / 72.6
+    mass interface: different left and right leads, two transverse k."""
+    b, E, p, aux = S.diamond_phonon(nc=2, L=6, nk_side=8, ne=24, kpoints=[5, 27], block=3)
+    Es = E[2:22:3]
+    q = np.repeat(np.arange(2, dtype=np.int32), Es.size)
+    check_against_oracle(b, np.tile(Es, 2), p, qidx=q)
+
+
+def test_tiled_diamond_blocked(cuda_ready):
+    """3 x 3 cells: n = 216, blocked inverse (six panels of 32, one of 24)."""
+    b, E, p, aux = S.diamond_phonon(nc=3, L=3, nk_side=8, ne=12, kpoints=[9], block=2)
+    bq = {k: v[0] for k, v in b.items()}
+    check_against_oracle(bq, E[3:9:2], p)
