@@ -338,11 +338,15 @@ const char* pf_modes_last_error(void);
  * grouped by q and advanced in batches through batched tile kernels (block
  * GEMMs, a blocked Gauss-Jordan inverse, masked decimation steps).  The call
  * is synchronous with respect to `stream` (the decimation loop reads one
- * counter per step).  work: pf_transport_tdb_tiled_workspace_size bytes.
+ * counter per step).  arith: PF_ARITH_FP64, or PF_ARITH_DF64 (every block
+ * operation in double-float pairs on the FP32 pipe, ~48 significant bits;
+ * the q block set is converted once into the workspace).
+ * work: pf_transport_tdb_tiled_workspace_size bytes.
  */
 #define PF_NMAX_TILED 2048
 
-size_t pf_transport_tdb_tiled_workspace_size(int n, int nl, int nr, int nq, int npts);
+size_t pf_transport_tdb_tiled_workspace_size(int n, int nl, int nr, int L, int nq,
+                                             int npts, int arith);
 
 int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq,
                                const double* HL, const double* HLv,
@@ -352,7 +356,7 @@ int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq,
                                int npts, const double* E, const int* qidx,
                                const int* zero_flag,
                                double eta, double eta0, double dev_factor,
-                               double convergence, int max_iter,
+                               double convergence, int max_iter, int arith,
                                double* transl, int* status, int* iters,
                                void* work, size_t work_bytes, void* stream);
 

@@ -49,8 +49,11 @@ template <typename T, bool CA, bool CB>
 __global__ void __launch_bounds__(GT) bgemm(GemmArgs<T> g) {
   const int b = blockIdx.z;
   if (g.active && !g.active[b]) return;
-  __shared__ cx<T> sa[BK][BM + 1];
-  __shared__ cx<T> sb[BK][BN + 1];
+  // raw storage: cx<df64> has a constructor, shared arrays must not
+  __shared__ __align__(16) unsigned char sa_raw[BK * (BM + 1) * sizeof(cx<T>)];
+  __shared__ __align__(16) unsigned char sb_raw[BK * (BN + 1) * sizeof(cx<T>)];
+  auto sa = reinterpret_cast<cx<T>(*)[BM + 1]>(sa_raw);
+  auto sb = reinterpret_cast<cx<T>(*)[BN + 1]>(sb_raw);
   const cx<T>* A = g.A + (size_t)b * g.sA;
   const cx<T>* B = g.B + (size_t)b * g.sB;
   cx<T>* C = g.C + (size_t)b * g.sC;
@@ -173,7 +176,8 @@ __global__ void __launch_bounds__(256) gje_panel(cx<T>* A, int lda, long long sA
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* S = reinterpret_cast<cx<T>*>(smem_raw);  // n x nb, ld = n
   cx<T>* colc = S + (size_t)n * nb;               // pivot column of the current step
-  __shared__ cx<T> prow[64];
+  __shared__ __align__(16) unsigned char prow_raw[64 * sizeof(cx<T>)];
+  cx<T>* prow = reinterpret_cast<cx<T>*>(prow_raw);
   __shared__ double rbest[8];
   __shared__ int ridx[8];
   __shared__ int s_p;

@@ -44,13 +44,32 @@ constexpr size_t kSmallInvBytes = 200 * 1024;
 constexpr size_t kPanelBytes = 200 * 1024;
 constexpr int kMats = 16;  // per-point working matrices
 
-// complex constant for host code (pf::mk is device-only)
+// complex constant for host code (pf::mk and df64(int) are device-only)
 template <typename T>
 __host__ __device__ inline cx<T> hmk(T a, T b) {
   cx<T> z;
   z.x = a;
   z.y = b;
   return z;
+}
+template <typename T>
+inline T hval(double v);
+template <>
+inline double hval<double>(double v) {
+  return v;
+}
+template <>
+inline pf::df64 hval<pf::df64>(double v) {  // exact for the constants used here (0, 1, -1)
+  return pf::df64((float)v, 0.f);
+}
+template <typename T>
+inline cx<T> hc(double re) {
+  return hmk<T>(hval<T>(re), hval<T>(0.0));
+}
+
+__global__ void k_to_df64(const double* __restrict__ src, pf::df64* __restrict__ dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = pf::df64(src[i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -141,7 +160,7 @@ __global__ void k_converge(const cx<T>* al, long long stride, int m, int ld, dou
   double v = 0.0;
   for (int i = threadIdx.x; i < m * m; i += blockDim.x) {
     const cx<T> e = al[(size_t)b * stride + (i % m) + (size_t)(i / m) * ld];
-    const double h = hypot((double)e.x, (double)e.y);
+    const double h = hypot(pf::to_d(e.x), pf::to_d(e.y));
     v = (h > v || h != h) ? h : v;
   }
   __shared__ double red[32];
@@ -179,7 +198,7 @@ __global__ void k_trace(const cx<T>* P, const cx<T>* Q, long long stride, int m,
     const int r = i % m, c = i / m;
     const cx<T> a = P[(size_t)b * stride + r + (size_t)c * ld];
     const cx<T> q = Q[(size_t)b * stride + c + (size_t)r * ld];
-    v += (double)a.x * (double)q.x - (double)a.y * (double)q.y;
+    v += pf::to_d(a.x) * pf::to_d(q.x) - pf::to_d(a.y) * pf::to_d(q.y);
   }
   __shared__ double red[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -343,7 +362,7 @@ struct Engine {
     const int nb = L.nb;
     const size_t psm = ((size_t)n * nb + n) * sizeof(cx<T>);
     TL_CUDA(cudaFuncSetAttribute(gje_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm));
-    const cx<T> one = hmk<T>(T(1), T(0)), zero = hmk<T>(T(0), T(0));
+    const cx<T> one = hc<T>(1.0), zero = hc<T>(0.0);
     for (int k = 0; k < n; k += nb) {
       const int kb = std::min(nb, n - k);
       gje_panel<T><<<B, 256, psm, s>>>(A, ld, sA, n, k, kb, w.piv, w.P, w.M11, active, w.st);
@@ -378,7 +397,7 @@ struct Engine {
     cx<T>* TT = w.mats[7];
     cx<T>* aln = w.mats[8];
     cx<T>* ben = w.mats[9];
-    const cx<T> one = hmk<T>(T(1), T(0)), zero = hmk<T>(T(0), T(0));
+    const cx<T> one = hc<T>(1.0), zero = hc<T>(0.0);
     k_copy<T><<<eg(m * m), 256, 0, s>>>(e1, sm, h00, 0, m, m, m, ld, 0);
     k_copy<T><<<eg(m * m), 256, 0, s>>>(es, sm, h00, 0, m, m, m, ld, 0);
     k_copy<T><<<eg(m * m), 256, 0, s>>>(al, sm, v, 0, m, m, m, ld, 1);
@@ -414,19 +433,19 @@ struct Engine {
   }
 
   // One batch of points sharing block set q: leads, sweep, Caroli.
-  int run(const pf::System<double>& sys, int q, const double* E, int cnt, double eta, double eta0, double devf,
+  int run(const pf::System<T>& sys, int q, const double* E, int cnt, double eta, double eta0, double devf,
           double conv, int max_iter, bool mirror, const int* zero_flag, double* transl, int* status, int* iters) {
     const int n = L.n, nl = L.nl, nr = L.nr, Ld = sys.L, ld = L.m;
     const long long sm = (long long)L.mat;
-    const cx<T> one = hmk<T>(T(1), T(0)), zero = hmk<T>(T(0), T(0)), mone = hmk<T>(T(-1), T(0));
-    const cx<T>* HL = reinterpret_cast<const cx<T>*>(sys.HL) + (size_t)q * nl * nl;
-    const cx<T>* HLv = reinterpret_cast<const cx<T>*>(sys.HLv) + (size_t)q * nl * nl;
-    const cx<T>* HR = reinterpret_cast<const cx<T>*>(sys.HR) + (size_t)q * nr * nr;
-    const cx<T>* HRv = reinterpret_cast<const cx<T>*>(sys.HRv) + (size_t)q * nr * nr;
-    const cx<T>* Hd = reinterpret_cast<const cx<T>*>(sys.Hd) + (size_t)q * Ld * n * n;
-    const cx<T>* Hdv = reinterpret_cast<const cx<T>*>(sys.Hdv) + (size_t)q * (Ld > 1 ? Ld - 1 : 0) * n * n;
-    const cx<T>* Hld = reinterpret_cast<const cx<T>*>(sys.Hld) + (size_t)q * nl * n;
-    const cx<T>* Hrd = reinterpret_cast<const cx<T>*>(sys.Hrd) + (size_t)q * nr * n;
+    const cx<T> one = hc<T>(1.0), zero = hc<T>(0.0), mone = hc<T>(-1.0);
+    const cx<T>* HL = sys.HL + (size_t)q * nl * nl;
+    const cx<T>* HLv = sys.HLv + (size_t)q * nl * nl;
+    const cx<T>* HR = sys.HR + (size_t)q * nr * nr;
+    const cx<T>* HRv = sys.HRv + (size_t)q * nr * nr;
+    const cx<T>* Hd = sys.Hd + (size_t)q * Ld * n * n;
+    const cx<T>* Hdv = sys.Hdv + (size_t)q * (Ld > 1 ? Ld - 1 : 0) * n * n;
+    const cx<T>* Hld = sys.Hld + (size_t)q * nl * n;
+    const cx<T>* Hrd = sys.Hrd + (size_t)q * nr * n;
     k_points<T><<<(cnt + 127) / 128, 128, 0, s>>>(E, w.idx, cnt, eta, eta0, devf, w.zl, w.zr, w.zd, w.st);
     TL_CUDA(cudaGetLastError());
     cx<T>* gl = w.mats[10];
@@ -500,47 +519,31 @@ struct Engine {
   }
 };
 
-}  // namespace
-
-extern "C" {
-
-const char* pf_tiled_last_error(void) { return g_err; }
-
-size_t pf_transport_tdb_tiled_workspace_size(int n, int nl, int nr, int nq, int npts) {
-  if (n <= 0 || nl <= 0 || nr <= 0 || nq <= 0 || npts < 0) return 0;
-  if (n > PF_NMAX_TILED || nl > PF_NMAX_TILED || nr > PF_NMAX_TILED) return 0;
-  const TLayout L = tlayout(n, nl, nr, npts, sizeof(cx<double>));
-  Work<double> w;
-  return 256 + carve<double>(nullptr, L, &w);
+// bytes of one q's blocks converted to double-float (0 for FP64)
+size_t conv_bytes(int n, int nl, int nr, int L, int arith) {
+  if (arith != PF_ARITH_DF64) return 0;
+  const size_t c = 2 * (size_t)nl * nl + 2 * (size_t)nr * nr + (size_t)L * n * n + (size_t)(L > 1 ? L - 1 : 0) * n * n +
+                   (size_t)nl * n + (size_t)nr * n;
+  return round256(c * 16);
 }
 
-int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
-                               const double* HR, const double* HRv, const double* Hd, const double* Hdv,
-                               const double* Hld, const double* Hrd, int npts, const double* E, const int* qidx,
-                               const int* zero_flag, double eta, double eta0, double dev_factor, double convergence,
-                               int max_iter, double* transl, int* status, int* iters, void* work,
-                               size_t work_bytes, void* stream) {
-  if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0)
-    return set_err(PF_ERR_ARG, "pf_tiled: dimensions must be positive");
-  if (n > PF_NMAX_TILED || nl > PF_NMAX_TILED || nr > PF_NMAX_TILED)
-    return set_err(PF_ERR_SIZE, "pf_tiled: block size exceeds PF_NMAX_TILED");
-  if (!HL || !HLv || !HR || !HRv || !Hd || !Hld || !Hrd || (L > 1 && !Hdv))
-    return set_err(PF_ERR_ARG, "pf_tiled: null block pointer");
-  if (!E || !transl || !status) return set_err(PF_ERR_ARG, "pf_tiled: null pointer");
-  if (max_iter <= 0) return set_err(PF_ERR_ARG, "pf_tiled: max_iter must be positive");
-  if (npts == 0) return PF_SUCCESS;
-  Engine<double> e;
-  e.L = tlayout(n, nl, nr, npts, sizeof(cx<double>));
-  const size_t need = 256 + carve<double>(nullptr, e.L, &e.w);
-  if (!work || work_bytes < need) return set_err(PF_ERR_ARG, "pf_tiled: workspace too small");
-  cudaStream_t st = (cudaStream_t)stream;
-  char* base = reinterpret_cast<char*>(work);
+// Driver shared by both arithmetics: group by q, (convert,) run batches.
+template <typename T>
+int drive(int n, int nl, int nr, int L, int nq, const double* const blk[8], int npts, const double* E,
+          const int* qidx, const int* zero_flag, double eta, double eta0, double dev_factor, double convergence,
+          int max_iter, double* transl, int* status, int* iters, char* base, size_t work_bytes, cudaStream_t st,
+          int arith) {
+  Engine<T> e;
+  e.L = tlayout(n, nl, nr, npts, sizeof(cx<T>));
+  const size_t cb = conv_bytes(n, nl, nr, L, arith);
+  const size_t need = 256 + cb + carve<T>(nullptr, e.L, &e.w);
+  if (!base || work_bytes < need) return set_err(PF_ERR_ARG, "pf_tiled: workspace too small");
   int* mirror_dev = reinterpret_cast<int*>(base);  // 256-byte header
-  carve<double>(base + 256, e.L, &e.w);
+  pf::df64* conv = reinterpret_cast<pf::df64*>(base + 256);
+  carve<T>(base + 256 + cb, e.L, &e.w);
   e.s = st;
   int host_count = 0;
   e.host_count = &host_count;
-  // group the points by q (host copy of qidx)
   std::vector<int> q(npts, 0);
   if (qidx) {
     TL_CUDA(cudaStreamSynchronize(st));
@@ -551,20 +554,9 @@ int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq, const doubl
   std::vector<int> order(npts);
   for (int i = 0; i < npts; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return q[a] < q[b]; });
-  pf::System<double> sys;
-  sys.n = n;
-  sys.nl = nl;
-  sys.nr = nr;
-  sys.L = L;
-  sys.nq = nq;
-  sys.HL = reinterpret_cast<const cx<double>*>(HL);
-  sys.HLv = reinterpret_cast<const cx<double>*>(HLv);
-  sys.HR = reinterpret_cast<const cx<double>*>(HR);
-  sys.HRv = reinterpret_cast<const cx<double>*>(HRv);
-  sys.Hd = reinterpret_cast<const cx<double>*>(Hd);
-  sys.Hdv = reinterpret_cast<const cx<double>*>(Hdv);
-  sys.Hld = reinterpret_cast<const cx<double>*>(Hld);
-  sys.Hrd = reinterpret_cast<const cx<double>*>(Hrd);
+  // per-q element counts of the eight block arrays (complex entries)
+  const size_t cnt_q[8] = {(size_t)nl * nl, (size_t)nl * nl, (size_t)nr * nr, (size_t)nr * nr, (size_t)L * n * n,
+                           (size_t)(L > 1 ? L - 1 : 0) * n * n, (size_t)nl * n, (size_t)nr * n};
   size_t i0 = 0;
   while (i0 < (size_t)npts) {
     const int qq = q[order[i0]];
@@ -574,12 +566,37 @@ int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq, const doubl
     if (nl == nr) {
       k_fill<<<1, 32, 0, st>>>(mirror_dev, 1, 0);
       const size_t off = (size_t)qq * nl * nl * 2;
-      k_mirror<<<64, 256, 0, st>>>(HL + off, HLv + off, HR + off, HRv + off, (size_t)nl * nl * 2, mirror_dev);
+      k_mirror<<<64, 256, 0, st>>>(blk[0] + off, blk[1] + off, blk[2] + off, blk[3] + off, (size_t)nl * nl * 2,
+                                   mirror_dev);
       TL_CUDA(cudaGetLastError());
       TL_CUDA(cudaStreamSynchronize(st));
       int diff = 1;
       TL_CUDA(cudaMemcpy(&diff, mirror_dev, sizeof(int), cudaMemcpyDeviceToHost));
       mirror = (diff == 0);
+    }
+    // the block set of this q, in the engine's arithmetic
+    pf::System<T> sys;
+    sys.n = n;
+    sys.nl = nl;
+    sys.nr = nr;
+    sys.L = L;
+    sys.nq = 1;
+    const cx<T>** dst[8] = {&sys.HL, &sys.HLv, &sys.HR, &sys.HRv, &sys.Hd, &sys.Hdv, &sys.Hld, &sys.Hrd};
+    pf::df64* c = conv;
+    for (int k = 0; k < 8; ++k) {
+      const double* src = blk[k] ? blk[k] + 2 * cnt_q[k] * (size_t)qq : nullptr;
+      if (arith == PF_ARITH_DF64) {
+        if (cnt_q[k]) {
+          const size_t nd = 2 * cnt_q[k];
+          const unsigned g = (unsigned)std::min<size_t>((nd + 255) / 256, 4096);
+          k_to_df64<<<g, 256, 0, st>>>(src, c, nd);
+          TL_CUDA(cudaGetLastError());
+        }
+        *dst[k] = reinterpret_cast<const cx<T>*>(c);
+        c += 2 * cnt_q[k];
+      } else {
+        *dst[k] = reinterpret_cast<const cx<T>*>(src);
+      }
     }
     for (size_t c0 = i0; c0 < i1; c0 += (size_t)e.L.batch) {
       const int cnt = (int)std::min((size_t)e.L.batch, i1 - c0);
@@ -591,7 +608,7 @@ int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq, const doubl
         TL_CUDA(cudaMemcpy(e.w.idx, order.data() + c0, sizeof(int) * cnt, cudaMemcpyHostToDevice));
       }
       e.B = cnt;
-      const int rc = e.run(sys, qq, E, cnt, eta, eta0, dev_factor, convergence, max_iter, mirror, zero_flag, transl,
+      const int rc = e.run(sys, 0, E, cnt, eta, eta0, dev_factor, convergence, max_iter, mirror, zero_flag, transl,
                            status, iters);
       if (rc) return rc;
     }
@@ -599,6 +616,52 @@ int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq, const doubl
   }
   TL_CUDA(cudaStreamSynchronize(st));
   return PF_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pf_tiled_last_error(void) { return g_err; }
+
+size_t pf_transport_tdb_tiled_workspace_size(int n, int nl, int nr, int L, int nq, int npts, int arith) {
+  if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0) return 0;
+  if (n > PF_NMAX_TILED || nl > PF_NMAX_TILED || nr > PF_NMAX_TILED) return 0;
+  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64) return 0;
+  const TLayout L2 = tlayout(n, nl, nr, npts, 16);
+  const size_t cb = conv_bytes(n, nl, nr, L, arith);
+  if (arith == PF_ARITH_FP64) {
+    Work<double> w;
+    return 256 + cb + carve<double>(nullptr, L2, &w);
+  }
+  Work<pf::df64> w;
+  return 256 + cb + carve<pf::df64>(nullptr, L2, &w);
+}
+
+int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
+                               const double* HR, const double* HRv, const double* Hd, const double* Hdv,
+                               const double* Hld, const double* Hrd, int npts, const double* E, const int* qidx,
+                               const int* zero_flag, double eta, double eta0, double dev_factor, double convergence,
+                               int max_iter, int arith, double* transl, int* status, int* iters, void* work,
+                               size_t work_bytes, void* stream) {
+  if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0)
+    return set_err(PF_ERR_ARG, "pf_tiled: dimensions must be positive");
+  if (n > PF_NMAX_TILED || nl > PF_NMAX_TILED || nr > PF_NMAX_TILED)
+    return set_err(PF_ERR_SIZE, "pf_tiled: block size exceeds PF_NMAX_TILED");
+  if (!HL || !HLv || !HR || !HRv || !Hd || !Hld || !Hrd || (L > 1 && !Hdv))
+    return set_err(PF_ERR_ARG, "pf_tiled: null block pointer");
+  if (!E || !transl || !status) return set_err(PF_ERR_ARG, "pf_tiled: null pointer");
+  if (max_iter <= 0) return set_err(PF_ERR_ARG, "pf_tiled: max_iter must be positive");
+  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64) return set_err(PF_ERR_ARG, "pf_tiled: unknown arithmetic");
+  if (npts == 0) return PF_SUCCESS;
+  const double* blk[8] = {HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd};
+  cudaStream_t st = (cudaStream_t)stream;
+  char* base = reinterpret_cast<char*>(work);
+  if (arith == PF_ARITH_FP64)
+    return drive<double>(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence,
+                         max_iter, transl, status, iters, base, work_bytes, st, arith);
+  return drive<pf::df64>(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence,
+                         max_iter, transl, status, iters, base, work_bytes, st, arith);
 }
 
 }  // extern "C"

@@ -86,12 +86,12 @@ NMAX_RESIDENT = 48   # PF_NMAX_RESIDENT
 def _transport_tiled(E, nq, dims, arrs, *, eta, eta0, convergence, dev_factor, qidx, zero_flag, max_iter,
                      want_transr, check, precision):
     """Blocks above the resident size: pf_transport_tdb_tiled_dev on torch
-    device buffers (T_L only, FP64)."""
+    device buffers (T_L only).  precision "mixed" selects the double-float
+    arithmetic of the tiled engine (FP32 pipe, ~48-bit)."""
     import torch
     if want_transr:
         raise ValueError("T_R is not computed for blocks above 48 (pass want_transr=False)")
-    if precision != "fp64":
-        raise ValueError("blocks above 48 run in FP64 (precision='fp64')")
+    arith = 0 if precision == "fp64" else 1   # PF_ARITH_FP64 / PF_ARITH_DF64
     lib = _abi.load()
     n, nl, nr, L = dims
     dev = {k: torch.from_numpy(fortran_block(v).copy()).cuda() for k, v in arrs.items()}
@@ -103,14 +103,14 @@ def _transport_tiled(E, nq, dims, arrs, *, eta, eta0, convergence, dev_factor, q
     tl = torch.zeros(max(npts, 1), dtype=torch.float64, device="cuda")
     st = torch.zeros(max(npts, 1), dtype=torch.int32, device="cuda")
     it = torch.zeros((max(npts, 1), 2), dtype=torch.int32, device="cuda")
-    ws = lib.pf_transport_tdb_tiled_workspace_size(n, nl, nr, nq, npts)
+    ws = lib.pf_transport_tdb_tiled_workspace_size(n, nl, nr, L, nq, npts, arith)
     if ws == 0:
         _abi.check(-3)
     work = torch.empty(ws, dtype=torch.uint8, device="cuda")
     p = lambda t: None if t is None else t.data_ptr()
     rc = lib.pf_transport_tdb_tiled_dev(n, nl, nr, L, nq, *[dev[k].data_ptr() for k in BLOCK_NAMES], npts,
                                         Ed.data_ptr(), p(qd), p(zd), eta, eta0, dev_factor, convergence, max_iter,
-                                        tl.data_ptr(), st.data_ptr(), it.data_ptr(), work.data_ptr(), ws,
+                                        arith, tl.data_ptr(), st.data_ptr(), it.data_ptr(), work.data_ptr(), ws,
                                         C.c_void_p(torch.cuda.current_stream().cuda_stream))
     if rc != 0:
         raise _abi.PFError(rc, lib.pf_tiled_last_error().decode(errors="replace"))

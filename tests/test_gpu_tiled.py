@@ -11,8 +11,8 @@ from phinfortran_gb300 import transport_tdb
 pytestmark = pytest.mark.gpu
 
 
-def check_against_oracle(b, E, p, qidx=None, zf=None, tol=1e-9):
-    r = transport_tdb(E, b, want_transr=False, qidx=qidx, zero_flag=zf, **p)
+def check_against_oracle(b, E, p, qidx=None, zf=None, tol=1e-9, precision="fp64"):
+    r = transport_tdb(E, b, want_transr=False, qidx=qidx, zero_flag=zf, precision=precision, **p)
     assert (r["status"] == 0).all()
     if qidx is None:
         o = N.transport(E, b, p["eta"], p["eta0"], p["convergence"], p["dev_factor"],
@@ -75,3 +75,13 @@ def test_tiled_diamond_blocked(cuda_ready):
     b, E, p, aux = S.diamond_phonon(nc=3, L=3, nk_side=8, ne=12, kpoints=[9], block=2)
     bq = {k: v[0] for k, v in b.items()}
     check_against_oracle(bq, E[3:9:2], p)
+
+
+@pytest.mark.parametrize("nc,kp", [(2, 27), (3, 9)])
+def test_tiled_double_float(cuda_ready, nc, kp):
+    """precision="mixed" above 48: the tiled engine in double-float
+    arithmetic (FP32 pipe); T within 1e-8 of the FP64 oracle (n = 96 and the
+    blocked inverse at n = 216)."""
+    b, E, p, aux = S.diamond_phonon(nc=nc, L=4, nk_side=8, ne=12, kpoints=[kp], block=2)
+    bq = {k: v[0] for k, v in b.items()}
+    check_against_oracle(bq, E[2:11:2], p, tol=1e-8, precision="mixed")
