@@ -258,3 +258,48 @@ def diamond_phonon(nc=2, L=60, nk_side=8, ne=512, k1=1.0, k2=0.2, masses=(28.0, 
     params = dict(eta=0.0, eta0=eta, dev_factor=10.0, convergence=convergence)
     aux = dict(kgrid=g, omega=w, omega_max=wmax, n=n, layer_mass=layer_mass)
     return blocks, w ** 2, params, aux
+
+
+def tb_ribbon3(W=256, L=1000, norb=3, onsite_sigma=0.3, hop_spread=0.1, ne=4096, emin=-4.2, emax=4.2, eta=1e-6,
+               convergence=1e-14, seed_index=5, energies=None):
+    """Multi-orbital nearest-neighbour square-lattice ribbon (electrons).
+
+    Width W sites with open edges and `norb` orbitals per site (n = W norb
+    per slice, orbital-major within a site).  Device slices: onsite energies
+    N(0, onsite_sigma^2) per orbital and every bond's hopping 1 + U[-spread,
+    spread] per orbital (orbital-diagonal); leads pristine (onsite 0,
+    hopping 1).  eta = 0, eta0 = eta, dev_factor = 1 as in the electron
+    driver; energies linear on [emin, emax] (``energies`` picks indices).
+    """
+    rng = _rng(seed_index)
+    n = W * norb
+    site = lambda i, o: i * norb + o
+
+    def slab(tv):
+        H = np.zeros((n, n), np.complex128)
+        for i in range(W - 1):
+            for o in range(norb):
+                H[site(i, o), site(i + 1, o)] = tv[i, o]
+                H[site(i + 1, o), site(i, o)] = tv[i, o]
+        return H
+
+    def coup(tz):
+        return np.diag(tz.reshape(-1)).astype(np.complex128)
+
+    ones_t = np.ones((W - 1, norb))
+    Hs = slab(ones_t)
+    Vz = coup(np.ones((W, norb)))
+    Hd = np.empty((L, n, n), np.complex128)
+    for j in range(L):
+        Hd[j] = slab(1.0 + rng.uniform(-hop_spread, hop_spread, size=(W - 1, norb)))
+        Hd[j][np.arange(n), np.arange(n)] += rng.normal(0.0, onsite_sigma, size=n)
+    Hdv = np.empty((max(L - 1, 0), n, n), np.complex128)
+    for j in range(L - 1):
+        Hdv[j] = coup(1.0 + rng.uniform(-hop_spread, hop_spread, size=(W, norb)))
+    blocks = dict(HL=Hs.copy(), HLv=Vz.copy(), HR=Hs.copy(), HRv=Vz.copy(), Hd=Hd, Hdv=Hdv, Hld=Vz.copy(),
+                  Hrd=Vz.copy())
+    E = emin + np.arange(ne) / max(ne - 1, 1) * (emax - emin)
+    if energies is not None:
+        E = E[np.asarray(energies)]
+    params = dict(eta=0.0, eta0=eta, dev_factor=1.0, convergence=convergence)
+    return blocks, E, params
