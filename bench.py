@@ -196,6 +196,39 @@ def time_steps(torch, fn, steps, flush, stream):
     return times
 
 
+def large_block_sample(torch):
+    """FP64 vs double-float tiled path on diamond-slab stacks (first+second
+    neighbour springs, 28 / 72.6 mass blocks of 10 layers, L = 60): n = 96
+    with 8 transverse k x 32 omega and n = 216 with 4 k x 8 omega."""
+    from phinfortran_gb300 import systems as S, transport_tdb
+    out = []
+    for nc, nk, ne in ((2, 8, 32), (3, 4, 8)):
+        kp = list(range(0, 64, 64 // nk))[:nk]
+        b, E, p, aux = S.diamond_phonon(nc=nc, L=60, kpoints=kp)
+        Es = E[np.linspace(10, 500, ne).astype(int)]
+        Eall = np.tile(Es, nk)
+        q = np.repeat(np.arange(nk, dtype=np.int32), ne)
+        res = {}
+        for prec in ("fp64", "mixed"):
+            transport_tdb(Eall[:1], b, qidx=q[:1], want_transr=False, precision=prec, **p)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = transport_tdb(Eall, b, qidx=q, want_transr=False, check=False, precision=prec, **p)
+            torch.cuda.synchronize()
+            res[prec] = (time.perf_counter() - t0, r)
+        n = aux["n"]
+        I = float(res["fp64"][1]["iters"][:, 0].mean())
+        fl = flops_per_solve(n, 60, I) * Eall.size
+        T64, Tm = res["fp64"][1]["transl"], res["mixed"][1]["transl"]
+        rel = np.abs(Tm - T64) / np.maximum(np.abs(T64), 1e-3)
+        out.append(dict(n=n, L=60, points=int(Eall.size), fp64_solves_per_s=Eall.size / res["fp64"][0],
+                        df64_solves_per_s=Eall.size / res["mixed"][0], df64_speedup=res["fp64"][0] / res["mixed"][0],
+                        fp64_tflops_algorithmic=fl / res["fp64"][0] / 1e12, mean_decimation_iters=I,
+                        df64_max_rel_dev_from_fp64=float(rel.max()),
+                        note="host-pointer call (blocks copied to the device inside the timed region)"))
+    return out
+
+
 def gradient_ratio(torch, flush, stream, steps):
     """Adjoint gradient (d kappa / d every block) vs one forward sweep on the
     simple-cubic 4x4x40 bar (n=48, L=40), masses U[1,3], springs U[0.8,1.2],
@@ -254,6 +287,7 @@ def main():
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the FP64 comparison path (accuracy and speed-up fields)")
     ap.add_argument("--no-grad", action="store_true", help="skip the gradient / forward cost ratio")
+    ap.add_argument("--no-large", action="store_true", help="skip the large-block (diamond slab) sample")
     ap.add_argument("--energies", type=int, default=0,
                     help="use only N energies of the workload (profiling runs)")
     args = ap.parse_args()
@@ -342,6 +376,11 @@ def main():
     if not args.no_grad:
         grad = gradient_ratio(torch, flush, stream, max(1, min(args.steps, 2)))
 
+    # ---- large blocks: diamond slab stacks (n = 96, 216; L = 60) ----
+    large = None
+    if not args.no_large:
+        large = large_block_sample(torch)
+
     # ---- end to end through the host-pointer C entry ----
     nq, dims, arrs = TdbBlocks.from_dict(b).stacked()
     h2d = sum(fortran_block(v).nbytes for v in arrs.values()) + E.nbytes
@@ -411,7 +450,7 @@ def main():
                             l2="flushed (256 MB write) before every timed step", parallelism=f"replicas x{ws}"),
                 e2e=dict(value=e2e_value, unit="solves/s", h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
                          entry="pf_transport_tdb_mixed" if args.path == "mixed" else "pf_transport_tdb"),
-                roofline=roof, cpu_baseline=cpu, compare=compare, gradient=grad,
+                roofline=roof, cpu_baseline=cpu, compare=compare, gradient=grad, large_blocks=large,
                 clocks=dict(sm_mhz=clk["sm_mhz"], sm_max_mhz=clk["sm_max_mhz"], reasons=clk["reasons"]),
                 gpu_launches=launches_per_step * args.steps, status_nonzero=int((status != 0).sum()))
     print(json.dumps(line), flush=True)

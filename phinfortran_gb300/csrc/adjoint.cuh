@@ -208,14 +208,15 @@ __device__ int adjoint_point(const Ctx<R>& c, const System<R>& sys, int q, cx<R>
 // ---------------------------------------------------------------------------
 // Checkpointed variant: memory O(sqrt(L)) instead of O(L) per point.
 //
-// Pass A (j = 0..L+1) forms the left-connected factors g_j, the forward
-// vectors y_j and the left-connected propagation G0_j = G^L_{0,j}
-// (G0_{L+1} = X_0), keeping (g_j, y_j) only at the checkpoints j = k*seg.
+// Pass A (j = 0..L+1) forms the left-connected factors g_j and the forward
+// vectors y_j, keeping (g_j, y_j) only at the checkpoints j = k*seg.  The
+// forward vectors are the left-connected propagators, y_j = (G^L_{0,j})^H,
+// so y_{L+1}^H = G_{0,L+1} = X_0 comes out of the same pass.
 // Pass B walks the segments from the right: it recomputes the segment's
 // g_j, y_j from its checkpoint and, layer by layer downwards, forms
 // X_j = g_j V_j X_{j+1}, Z_j = y_j + g_j^H V_j Z_{j+1}, K_j = X_j W and the
 // sensitivities.  Extra work over the store-all kernel: one recomputation
-// of the factors and the y vectors, plus the G0 propagation.
+// of the factors and the y vectors.
 // ---------------------------------------------------------------------------
 template <typename R>
 struct CkptSlabs {
@@ -225,7 +226,7 @@ struct CkptSlabs {
   cx<R>* segy;  // [seg] segment y vectors
   cx<R>* pg;    // pass A rolling g
   cx<R>* py;    // pass A rolling y
-  cx<R>* pG0;   // pass A rolling G0 (ends as X_0)
+  cx<R>* pG0;   // spare matrix (layout kept stable)
   cx<R>* W;     // Gamma_R X_0^H Gamma_L
   cx<R>* xa;    // X rolling pair
   cx<R>* xb;
@@ -283,7 +284,6 @@ __device__ int adjoint_point_ckpt(const Ctx<R>& c, const System<R>& sys, int q, 
   // ---- pass A
   copy_in(sl.pg, ld, opN<R>(c.gs[G_GL], ld), nl, nl);
   copy_in(sl.py, ld, opC<R>(c.gs[G_GL], ld), nl, nl);
-  copy_in(sl.pG0, ld, opN<R>(c.gs[G_GL], ld), nl, nl);
   copy_in(sl.ckg, ld, opN<R>(c.gs[G_GL], ld), nl, nl);
   copy_in(sl.cky, ld, opC<R>(c.gs[G_GL], ld), nl, nl);
   for (int j = 1; j <= L + 1; ++j) {
@@ -291,20 +291,17 @@ __device__ int adjoint_point_ckpt(const Ctx<R>& c, const System<R>& sys, int q, 
     // s0 = V_{j-1}, s1 = scratch, s2 = g_j; y_j -> py (its product reads s1, not py)
     st |= ckpt_step<R, S>(c, sys, q, zD, j, sl.pg, sl.py, s0, s1, s2, nullptr, s3);
     copy_out(sl.py, ld, false, s3, ld, dj, nl);
-    // G0_j = (G0_{j-1} V_{j-1}) g_j
-    row_gemm<R, S>(nl, dj, xdim(sys, j - 1), opN<R>(sl.pG0, ld), opN<R>(s0, ld), EpiStore<R>{s1, ld, mk<R>(1, 0)});
-    row_gemm<R, S>(nl, dj, dj, opN<R>(s1, ld), opN<R>(s2, ld), EpiStore<R>{sl.pG0, ld, mk<R>(1, 0)});
     copy_out(sl.pg, ld, false, s2, ld, dj, dj);
     if (j % seg == 0) {
       copy_out(sl.ckg + (size_t)(j / seg) * mat, ld, false, s2, ld, dj, dj);
       copy_out(sl.cky + (size_t)(j / seg) * mat, ld, false, s3, ld, dj, nl);
     }
   }
-  // ---- T and W from X_0 = G0_{L+1}
+  // ---- T and W from X_0 = G^L_{0,L+1} = y_{L+1}^H (py holds y_{L+1}, nr x nl)
   copy_in(s0, ld, opN<R>(c.gs[G_GMR], ld), nr, nr);
-  row_gemm<R, S>(nl, nr, nr, opN<R>(sl.pG0, ld), opN<R>(s0, ld), EpiStore<R>{s1, ld, mk<R>(1, 0)});  // P
+  row_gemm<R, S>(nl, nr, nr, opC<R>(sl.py, ld), opN<R>(s0, ld), EpiStore<R>{s1, ld, mk<R>(1, 0)});  // P
   copy_in(s2, ld, opN<R>(c.gs[G_GML], ld), nl, nl);
-  row_gemm<R, S>(nr, nl, nl, opC<R>(sl.pG0, ld), opN<R>(s2, ld), EpiStore<R>{s3, ld, mk<R>(1, 0)});  // Q
+  row_gemm<R, S>(nr, nl, nl, opN<R>(sl.py, ld), opN<R>(s2, ld), EpiStore<R>{s3, ld, mk<R>(1, 0)});  // Q
   *trans = trace_prod_re(s1, ld, opN<R>(s3, ld), nl, nr, c.red);
   row_gemm<R, S>(nr, nl, nr, opN<R>(s0, ld), opN<R>(s3, ld), EpiStore<R>{sl.W, ld, mk<R>(1, 0)});  // W
   // ---- pass B
