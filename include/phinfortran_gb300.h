@@ -363,6 +363,38 @@ int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq,
 /* Message for the last error of the large-block entry points. */
 const char* pf_tiled_last_error(void);
 
+/*
+ * Tight-binding H(k) blocks (replaces gen_ham / V_sk / V_term / onsite of
+ * tb/hamiltonian.f90:28-519 as used by gen_ham_mpi; the reference builds the
+ * dense norb x norb matrix, here only the blocks the transport entries
+ * take).  Atoms are grouped into nblk layers by blk_atom[0..nblk]
+ * (increasing atom boundaries); orbitals follow gen_ham's order (atom-major,
+ * then the species' orbital list).  For every k (fractional, kfrac[nk][3],
+ * Cartesian k = kfrac . recivec) `out` receives, as interleaved complex
+ * column-major blocks, first H_{I,I} for I = 0..nblk-1, then H_{I,I+1} for
+ * I = 0..nblk-2, of the Hermitised matrix 0.5 (H + H^H).
+ *   pos[natoms][3]   positions in Angstrom and r_d in metres, as the
+ *                    reference holds them (V_term = V (r_d / |r| / 1e-10)^Vn),
+ *                    species[natoms] 0-based
+ *   orb_codes[nspecies][PF_TB_MAX_ORB]: 0 s, 1 px, 2 py, 3 pz, 4 dxy,
+ *                    5 dyz, 6 dxz, 7 dx2-y2, 8 dz2, 9 s*
+ *   V, Vn[nspecies][nspecies][4][4][4] (C order; principal numbers s 1, p 2,
+ *                    d 3, s* 4; type 1 onsite, 2 sigma, 3 pi, 4 delta),
+ *   r_d[nspecies][nspecies], latvec / recivec rows = vectors.
+ * Host pointers; synchronous.
+ */
+#define PF_TB_MAX_ORB 10
+
+int pf_tb_hk_blocks(int natoms, const double* pos, const int* species,
+                    int nspecies, const int* norb_species, const int* orb_codes,
+                    const double* V, const double* Vn, const double* r_d,
+                    const double* latvec, const double* recivec,
+                    double r_cutoff, int nk, const double* kfrac, int nblk,
+                    const int* blk_atom, double* out);
+
+/* Message for the last error of pf_tb_hk_blocks. */
+const char* pf_tb_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,6 +89,9 @@ SIGNATURES = {
                                              C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
                                              C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_size_t, C.c_void_p]),
+    "pf_tb_last_error": (C.c_char_p, []),
+    "pf_tb_hk_blocks": (C.c_int, [C.c_int, _dp, _ip, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp, C.c_double,
+                                  C.c_int, _dp, C.c_int, _ip, _dp]),
     "pf_transport_tdb": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                    _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                    C.c_int, _dp, _ip, _ip,
