@@ -170,8 +170,12 @@ __global__ void __launch_bounds__(kPrepThreads)
                                     nullptr);
       pf::copy_out(ch.rec(lp, R_GLP), ld, false, c.sm[2], ld, nl, nl);
     }
-    // right "minus" (surface.f90:571-593): z = E - i eps, alpha = Hamrv, beta = Hamrv^H
-    {
+    // right "minus" (surface.f90:571-593): z = E - i eps, alpha = Hamrv, beta = Hamrv^H.
+    // Identical leads: the adjoint of the left "plus" problem, gr_minus = gl_plus^H
+    // (the relation lead_pair uses for gr_ret = gl_adv^H).
+    if (P.lead_mirror && P.lead_mirror[q]) {
+      pf::copy_out(ch.rec(lp, R_GRM), ld, true, ch.rec(lp, R_GLP), ld, nr, nr);
+    } else {
       const C* HR = sys.HR + (size_t)q * nr * nr;
       const C* HRv = sys.HRv + (size_t)q * nr * nr;
       st |= pf::decimate<double, S>(c, nr, pf::mk<double>(E, -eps), pf::opN<double>(HR, nr),
