@@ -414,7 +414,8 @@ __global__ void __launch_bounds__(kThreads) mixed_kernel(pf::MSys sys, pf::Point
 // Mixed path, cross-sections <= 32: leads kernel (CTA per point) + layer
 // kernel (warp per point).
 // ---------------------------------------------------------------------------
-constexpr int kWarpsPerCta = 8;
+constexpr int kWarpsPerCta = 4;
+constexpr int kLayerCtasPerSm = 3;  // 12 warps per SM: 2 x 8.5 KB shared buffers and <= 170 registers a thread
 
 // Copy an (m x m) df64/FP32 matrix from scratch (ld) into a padded 32x32
 // per-point block (ld 32); `ident` puts ones on the padded diagonal.
@@ -589,14 +590,15 @@ __global__ void residual_kernel(pf::MSys s, pf::Points pts, const dcx* z2, pf::w
   }
 }
 
-__global__ void __launch_bounds__(kWarpsPerCta * 32, 1)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, kLayerCtasPerSm)
     layer_kernel(pf::MSys sys, pf::Points pts, pf::Params P, int phase, pf::Outputs out, pf::wp::LeadOut lo,
                  pf::wp::Slabs sl, int* lead_status, int* queue) {
   using namespace pf::wp;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  fcx* G = reinterpret_cast<fcx*>(smem_raw) + (size_t)w * 2 * LDW * NW;
-  fcx* Vb = G + LDW * NW;
+  // two 32 x 32 FP32 buffers per warp
+  fcx* X = reinterpret_cast<fcx*>(smem_raw) + (size_t)w * 2 * LDW * NW;
+  fcx* Y = X + LDW * NW;
   const int L = sys.L, nr = sys.nr;
   const size_t B = (size_t)NW * NW;
   for (;;) {
@@ -613,111 +615,108 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 1)
     fcx* lu = sl.lu + (size_t)p * (L + 2) * B;
     fcx* yv = sl.yv + (size_t)p * (L + 2) * B;
     dcx* xv = sl.xv + (size_t)p * (L + 2) * B;
-    fcx a[NW], t[NW], u[NW];
+    fcx a[NW];
+    const auto to_df = [](fcx v) { return pf::mk<pf::df64>(pf::df64(v.x, 0.f), pf::df64(v.y, 0.f)); };
     if (do_factor) {
-    // ---- g_0 = gl (padded), kept in G and lu[0]
-    load_col(lo.g0 + p * B, NW, NW, NW, false, lane, a);
-    store_col_smem(G, lane, a);
-#pragma unroll
-    for (int r = 0; r < NW; ++r) lu[r + lane * NW] = a[r];
-    __syncwarp();
-    // ---- FP32 block LU, j = 1..L+1
-    for (int j = 1; j <= L + 1; ++j) {
-      const int dj = edim(sys, j);
-      stage_v(Vb, vview(sys, q, j - 1), lane);
-#pragma unroll
-      for (int r = 0; r < NW; ++r) a[r] = Vb[r + lane * LDW];
-      wgemm(G, a, t);                          // T = g_{j-1} V
-      wgemm_ct(Vb, t, u);                      // S = V^H T
-      const fcx* H = (j <= L) ? sys.fHd + ((size_t)q * L + (j - 1)) * sys.n * sys.n : sys.fHR + (size_t)q * nr * nr;
-      const int ldh = (j <= L) ? sys.n : nr;
-      const fcx* Sr = lo.fsr + p * B;
-#pragma unroll
-      for (int r = 0; r < NW; ++r) {
-        fcx v;
-        if (r < dj && lane < dj) {
-          v = pf::mk<float>(-u[r].x, -u[r].y);
-          if (r == lane) v = pf::cadd(v, zf);
-          v = pf::csub(v, H[r + (size_t)lane * ldh]);
-          if (j == L + 1) v = pf::csub(v, Sr[r + lane * NW]);
-        } else {
-          v = pf::mk<float>(r == lane ? 1.f : 0.f, 0.f);
-        }
-        a[r] = v;
+      // ---- g_0 = gl (padded), kept in X and lu[0]
+      const fcx* g0 = lo.g0 + p * B;
+      for (int c = 0; c < NW; ++c) {
+        const fcx v = g0[lane + c * NW];
+        X[lane + c * LDW] = v;
+        lu[lane + c * NW] = v;
       }
       __syncwarp();
-      store_col_smem(G, lane, a);
-      __syncwarp();
-      st |= winverse(G, Vb, lu + (size_t)j * B, lane);
-      fcx* tmp = G;
-      G = Vb;
-      Vb = tmp;
-    }
-    // ---- back substitution: X_{L+1} = g_{L+1}; X_j = g_j V_j X_{j+1}
-#pragma unroll
-    for (int r = 0; r < NW; ++r) a[r] = (lane < nr) ? G[r + lane * LDW] : fz();
-#pragma unroll
-    for (int r = 0; r < NW; ++r)
-      xv[(size_t)(L + 1) * B + r + lane * NW] = pf::mk<pf::df64>(pf::df64(a[r].x, 0.f), pf::df64(a[r].y, 0.f));
-    for (int j = L; j >= 0; --j) {
-      __syncwarp();
-      stage_v(Vb, vview(sys, q, j), lane);
-      wgemm(Vb, a, t);                         // W = V_j X_{j+1}
-      __syncwarp();
-      load_col(lu + (size_t)j * B, NW, NW, NW, false, lane, u);
-      store_col_smem(G, lane, u);
-      __syncwarp();
-      wgemm(G, t, a);                          // X_j = g_j W
-#pragma unroll
-      for (int r = 0; r < NW; ++r) {
-        if (lane >= nr) a[r] = fz();
-        xv[(size_t)j * B + r + lane * NW] = pf::mk<pf::df64>(pf::df64(a[r].x, 0.f), pf::df64(a[r].y, 0.f));
+      // ---- FP32 block LU, j = 1..L+1: A_j = z - H_j - V^H g_{j-1} V (- Sigma_R), g_j = A_j^-1
+      for (int j = 1; j <= L + 1; ++j) {
+        const int dj = edim(sys, j);
+        row_smem(X, lane, a);                                    // row of g_{j-1}
+        stage_rows(Y, vview(sys, q, j - 1), lane);                // V
+        __syncwarp();
+        rgemm(a, Y, lane, [&](int r, int c, fcx v) { X[r + c * LDW] = v; });  // T = g_{j-1} V
+        __syncwarp();
+        row_smem_h(Y, lane, a);                                  // row of V^H
+        __syncwarp();
+        const fcx* H = (j <= L) ? sys.fHd + ((size_t)q * L + (j - 1)) * sys.n * sys.n : sys.fHR + (size_t)q * nr * nr;
+        const int ldh = (j <= L) ? sys.n : nr;
+        const fcx* Sr = lo.fsr + p * B;
+        rgemm(a, X, lane, [&](int r, int c, fcx u) {             // A_j from V^H T
+          fcx v;
+          if (r < dj && c < dj) {
+            v = pf::mk<float>(-u.x, -u.y);
+            if (r == c) v = pf::cadd(v, zf);
+            v = pf::csub(v, H[r + (size_t)c * ldh]);
+            if (j == L + 1) v = pf::csub(v, Sr[r + c * NW]);
+          } else {
+            v = pf::mk<float>(r == c ? 1.f : 0.f, 0.f);
+          }
+          Y[r + c * LDW] = v;
+        });
+        __syncwarp();
+        st |= winverse(Y, X, lu + (size_t)j * B, lane);         // g_j -> X and lu[j]
       }
-    }
+      // ---- back substitution: X_{L+1} = g_{L+1}; X_j = g_j V_j X_{j+1} (columns >= nr are zero)
+      for (int c = 0; c < NW; ++c) {
+        const fcx v = c < nr ? X[lane + c * LDW] : fz();
+        X[lane + c * LDW] = v;
+        xv[(size_t)(L + 1) * B + lane + c * NW] = to_df(v);
+      }
+      __syncwarp();
+      for (int j = L; j >= 0; --j) {
+        row_view(vview(sys, q, j), lane, a);
+        rgemm(a, X, lane, [&](int r, int c, fcx v) { Y[r + c * LDW] = v; });  // W = V_j X_{j+1}
+        __syncwarp();
+        row_block(lu + (size_t)j * B, lane, a);
+        rgemm(a, Y, lane, [&](int r, int c, fcx v) {             // X_j = g_j W
+          if (c >= nr) v = fz();
+          X[r + c * LDW] = v;
+          xv[(size_t)j * B + r + c * NW] = to_df(v);
+        });
+        __syncwarp();
+      }
     }  // do_factor
     // ---- one refinement sweep (the residual r_j was written into yv[j] by residual_kernel)
     if (do_refine) {
-      // forward: y_j = g_j (r_j + V_{j-1}^H y_{j-1})
+      // forward: y_j = g_j (r_j + V_{j-1}^H y_{j-1}); y_{j-1} is kept in X
+      for (int c = 0; c < NW; ++c) Y[lane + c * LDW] = yv[lane + c * NW];
+      __syncwarp();
       for (int j = 0; j <= L + 1; ++j) {
-        __syncwarp();
-        load_col(yv + (size_t)j * B, NW, NW, NW, false, lane, u);
         if (j >= 1) {
-          stage_v(Vb, vview(sys, q, j - 1), lane);
-          wgemm_ct(Vb, a, t);                  // a holds y_{j-1}
-#pragma unroll
-          for (int r = 0; r < NW; ++r) u[r] = pf::cadd(u[r], t[r]);
+          stage_rows(Y, vview(sys, q, j - 1), lane);
+          __syncwarp();
+          row_smem_h(Y, lane, a);                                // row of V_{j-1}^H
+          __syncwarp();
+          rgemm(a, X, lane, [&](int r, int c, fcx v) {           // u = r_j + V^H y_{j-1}
+            Y[r + c * LDW] = pf::cadd(v, yv[(size_t)j * B + r + c * NW]);
+          });
+          __syncwarp();
         }
+        row_block(lu + (size_t)j * B, lane, a);
+        rgemm(a, Y, lane, [&](int r, int c, fcx v) {             // y_j = g_j u
+          X[r + c * LDW] = v;
+          yv[(size_t)j * B + r + c * NW] = v;
+        });
         __syncwarp();
-        load_col(lu + (size_t)j * B, NW, NW, NW, false, lane, t);
-        store_col_smem(G, lane, t);
-        __syncwarp();
-        wgemm(G, u, a);                        // y_j
-#pragma unroll
-        for (int r = 0; r < NW; ++r) yv[(size_t)j * B + r + lane * NW] = a[r];
       }
-      // backward: d_{L+1} = y_{L+1}; d_j = y_j + g_j V_j d_{j+1}; X += d
-#pragma unroll
-      for (int r = 0; r < NW; ++r) {
-        dcx& x = xv[(size_t)(L + 1) * B + r + lane * NW];
-        x.x = x.x + pf::df64(a[r].x, 0.f);
-        x.y = x.y + pf::df64(a[r].y, 0.f);
+      // backward: d_{L+1} = y_{L+1}; d_j = y_j + g_j V_j d_{j+1}; X += d (d_{j+1} kept in X)
+      for (int c = 0; c < NW; ++c) {
+        dcx& x = xv[(size_t)(L + 1) * B + lane + c * NW];
+        const fcx d = X[lane + c * LDW];
+        x.x = x.x + pf::df64(d.x, 0.f);
+        x.y = x.y + pf::df64(d.y, 0.f);
       }
       for (int j = L; j >= 0; --j) {
+        row_view(vview(sys, q, j), lane, a);
+        rgemm(a, X, lane, [&](int r, int c, fcx v) { Y[r + c * LDW] = v; });  // t = V_j d_{j+1}
         __syncwarp();
-        stage_v(Vb, vview(sys, q, j), lane);
-        wgemm(Vb, a, t);
+        row_block(lu + (size_t)j * B, lane, a);
+        rgemm(a, Y, lane, [&](int r, int c, fcx v) {             // d_j = y_j + g_j t
+          v = pf::cadd(v, yv[(size_t)j * B + r + c * NW]);
+          X[r + c * LDW] = v;
+          dcx& x = xv[(size_t)j * B + r + c * NW];
+          x.x = x.x + pf::df64(v.x, 0.f);
+          x.y = x.y + pf::df64(v.y, 0.f);
+        });
         __syncwarp();
-        load_col(lu + (size_t)j * B, NW, NW, NW, false, lane, u);
-        store_col_smem(G, lane, u);
-        __syncwarp();
-        wgemm(G, t, a);
-#pragma unroll
-        for (int r = 0; r < NW; ++r) {
-          a[r] = pf::cadd(a[r], yv[(size_t)j * B + r + lane * NW]);
-          dcx& x = xv[(size_t)j * B + r + lane * NW];
-          x.x = x.x + pf::df64(a[r].x, 0.f);
-          x.y = x.y + pf::df64(a[r].y, 0.f);
-        }
       }
     }
     if (do_factor) {

@@ -5,10 +5,12 @@
 // back substitution of the last block column, double-float residual
 // refinement and the double-float Caroli trace -- runs with ONE WARP PER
 // POINT and no CTA barriers:
-//   * lane c owns column c of the right-hand operand and of the result, in
-//     registers (32 complex floats);
-//   * the left operand of every product lives in the warp's own shared
-//     memory and is read by broadcast (all lanes read the same element);
+//   * lane r holds row r of the left operand of a product in registers (32
+//     complex floats), loaded from global memory (coalesced across lanes) or
+//     from the warp's shared memory;
+//   * the right operand lives in one of the warp's two shared 32 x 32
+//     buffers and is read by broadcast; results go back to shared memory
+//     (and to the per-point slabs) column by column;
 //   * the block inverse is an in-shared-memory Gauss-Jordan with implicit
 //     partial pivoting (no row exchanges; the final permutation is applied
 //     when the factor is stored: inv(A)[k, P[j]] = M[P[k], j]).
@@ -44,52 +46,56 @@ struct Slabs {
 __device__ __forceinline__ fcx fz() { return mk<float>(0.f, 0.f); }
 __device__ __forceinline__ fcx ffma(fcx a, fcx b, fcx c) { return cfma(a, b, c); }
 
-// c[:] = A(smem, ld LDW) * b[:]   (lane's column)
-__device__ __forceinline__ void wgemm(const fcx* A, const fcx (&b)[NW], fcx (&c)[NW]) {
+// Products are row-stationary: lane r holds row r of the left operand in
+// registers (32 complex floats), the right operand sits in the warp's shared
+// memory and is read by broadcast, and the result goes to an epilogue
+// functor element by element (lane r, column c).  The column loop is not
+// unrolled, so one product is a few hundred instructions of code: the
+// layer loops stay resident in the instruction cache (a fully unrolled
+// 32 x 32 x 32 product is ~75 KB of code per call site).
+
+// a[k] = S(lane, k) of a shared-memory block (ld LDW)
+__device__ __forceinline__ void row_smem(const fcx* S, int lane, fcx (&a)[NW]) {
 #pragma unroll
-  for (int r = 0; r < NW; ++r) c[r] = fz();
+  for (int k = 0; k < NW; ++k) a[k] = S[lane + k * LDW];
+}
+// a[k] = conj(S(k, lane)): row `lane` of S^H
+__device__ __forceinline__ void row_smem_h(const fcx* S, int lane, fcx (&a)[NW]) {
+  const float4* col = reinterpret_cast<const float4*>(S + lane * LDW);
 #pragma unroll
-  for (int k = 0; k < NW; ++k) {
-    const fcx bk = b[k];
-    const float4* col = reinterpret_cast<const float4*>(A + k * LDW);
-#pragma unroll
-    for (int r2 = 0; r2 < NW / 2; ++r2) {
-      const float4 a = col[r2];
-      c[2 * r2] = ffma(mk<float>(a.x, a.y), bk, c[2 * r2]);
-      c[2 * r2 + 1] = ffma(mk<float>(a.z, a.w), bk, c[2 * r2 + 1]);
-    }
+  for (int k2 = 0; k2 < NW / 2; ++k2) {
+    const float4 v = col[k2];
+    a[2 * k2] = mk<float>(v.x, -v.y);
+    a[2 * k2 + 1] = mk<float>(v.z, -v.w);
   }
 }
-// c[:] = A^H * b[:]   (A in smem; row k of A read as column k of A^H)
-__device__ __forceinline__ void wgemm_ct(const fcx* A, const fcx (&b)[NW], fcx (&c)[NW]) {
+// a[k] = M(lane, k) of a padded global block (ld NW)
+__device__ __forceinline__ void row_block(const fcx* M, int lane, fcx (&a)[NW]) {
 #pragma unroll
-  for (int r = 0; r < NW; ++r) c[r] = fz();
-#pragma unroll
-  for (int k = 0; k < NW; ++k) {
-    const fcx bk = b[k];
-#pragma unroll
-    for (int r = 0; r < NW; ++r) c[r] = ffma(cconj(A[k + r * LDW]), bk, c[r]);
-  }
+  for (int k = 0; k < NW; ++k) a[k] = M[lane + k * NW];
 }
 
-// Lane c loads column c of an (rows x cols) column-major global block with
-// leading dimension ldg (zero padding), optionally conjugate-transposed.
-__device__ __forceinline__ void load_col(const fcx* M, int ldg, int rows, int cols, bool ct, int c, fcx (&v)[NW]) {
+// For c = 0..31: epi(lane, c, sum_k a[k] B(k, c)), B in shared memory (ld LDW).
+template <class Epi>
+__device__ __forceinline__ void rgemm(const fcx (&a)[NW], const fcx* B, int lane, Epi epi) {
+  constexpr int U = 4;  // columns per step: 8 independent FMA chains per lane
+#pragma unroll 1
+  for (int c0 = 0; c0 < NW; c0 += U) {
+    fcx acc0[U], acc1[U];
 #pragma unroll
-  for (int r = 0; r < NW; ++r) {
-    fcx e = fz();
-    if (!ct) {
-      if (r < rows && c < cols) e = M[r + (size_t)c * ldg];
-    } else {
-      // element (r, c) of M^H = conj(M(c, r)); M is cols x rows here
-      if (r < rows && c < cols) e = cconj(M[c + (size_t)r * ldg]);
+    for (int u = 0; u < U; ++u) acc0[u] = acc1[u] = fz();
+#pragma unroll
+    for (int k = 0; k < NW; k += 2) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const float4 b = *reinterpret_cast<const float4*>(B + k + (c0 + u) * LDW);
+        acc0[u] = ffma(a[k], mk<float>(b.x, b.y), acc0[u]);
+        acc1[u] = ffma(a[k + 1], mk<float>(b.z, b.w), acc1[u]);
+      }
     }
-    v[r] = e;
-  }
-}
-__device__ __forceinline__ void store_col_smem(fcx* S, int c, const fcx (&v)[NW]) {
 #pragma unroll
-  for (int r = 0; r < NW; ++r) S[r + c * LDW] = v[r];
+    for (int u = 0; u < U; ++u) epi(lane, c0 + u, cadd(acc0[u], acc1[u]));
+  }
 }
 
 // Operand V_j (dims dj x d(j+1)) of the extended system as a global view.
@@ -122,12 +128,28 @@ __device__ __forceinline__ GView vview(const MSys& s, int q, int j) {
   }
   return g;
 }
-// Stage V_j into the warp's smem buffer (lane c writes column c).
-__device__ __forceinline__ void stage_v(fcx* S, const GView& g, int c) {
-  fcx v[NW];
-  load_col(g.p, g.ldg, g.rows, g.cols, g.ct, c, v);
-  store_col_smem(S, c, v);
-  __syncwarp();
+__device__ __forceinline__ GView vview_h(const MSys& s, int q, int j) {
+  GView g = vview(s, q, j);
+  const int t = g.rows;
+  g.rows = g.cols;
+  g.cols = t;
+  g.ct = !g.ct;
+  return g;
+}
+// Element (r, k) of a view (zero outside rows x cols).
+__device__ __forceinline__ fcx view_at(const GView& g, int r, int k) {
+  if (r >= g.rows || k >= g.cols) return fz();
+  return g.ct ? cconj(g.p[k + (size_t)r * g.ldg]) : g.p[r + (size_t)k * g.ldg];
+}
+// a[k] = g(lane, k)
+__device__ __forceinline__ void row_view(const GView& g, int lane, fcx (&a)[NW]) {
+#pragma unroll
+  for (int k = 0; k < NW; ++k) a[k] = view_at(g, lane, k);
+}
+// Stage a view into the warp's smem buffer (lane r writes row r).
+__device__ __forceinline__ void stage_rows(fcx* S, const GView& g, int lane) {
+#pragma unroll
+  for (int k = 0; k < NW; ++k) S[lane + k * LDW] = view_at(g, lane, k);
 }
 
 // In-place Gauss-Jordan inverse of the 32x32 matrix in S with implicit
@@ -165,21 +187,17 @@ __device__ int winverse(fcx* S, fcx* D, fcx* gout, int lane) {
     for (int r = 0; r < NW; ++r) colk[r] = S[r + k * LDW];
     const fcx rowp = S[p + lane * LDW];
     __syncwarp();
-    if (lane == k) {
+    // column k becomes -col_k / piv (ip on the pivot row), every other
+    // column c becomes col_c - col_k f_c with f_c = S(p, c) / piv: one
+    // update for all lanes, with (old, f) = (0, ip) on lane k
+    const bool pivcol = lane == k;
+    const fcx f = pivcol ? ip : cmul(rowp, ip);
 #pragma unroll
-      for (int r = 0; r < NW; ++r) {
-        const fcx t = cmul(colk[r], ip);
-        S[r + k * LDW] = (r == p) ? ip : mk<float>(-t.x, -t.y);
-      }
-    } else {
-      const fcx f = cmul(rowp, ip);
-#pragma unroll
-      for (int r = 0; r < NW; ++r) {
-        const fcx old = S[r + lane * LDW];
-        const fcx nv = mk<float>(old.x - (colk[r].x * f.x - colk[r].y * f.y),
-                                 old.y - (colk[r].x * f.y + colk[r].y * f.x));
-        S[r + lane * LDW] = (r == p) ? f : nv;
-      }
+    for (int r = 0; r < NW; ++r) {
+      const fcx old = pivcol ? fz() : S[r + lane * LDW];
+      const fcx nv = mk<float>(old.x - (colk[r].x * f.x - colk[r].y * f.y),
+                               old.y - (colk[r].x * f.y + colk[r].y * f.x));
+      S[r + lane * LDW] = (r == p) ? f : nv;
     }
     used |= 1u << p;
     __syncwarp();
