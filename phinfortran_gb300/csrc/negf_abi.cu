@@ -306,6 +306,7 @@ __global__ void build_ell_kernel(const dcx* M, int rows, int cols, int count, in
 struct MixedLayout {
   Layout base;     // smem slots are df64-sized (16 B per complex)
   size_t smem;
+  size_t smem_leads;  // the leads kernel needs only the NSM decimation slots
   size_t per_cta;  // bytes of per-CTA scratch
   size_t blocks_d, blocks_f;  // bytes of converted block copies (per call)
   size_t cnt[8];   // complex elements per block family (all q)
@@ -317,8 +318,10 @@ MixedLayout make_mixed_layout(int n, int nl, int nr, int L, int nq) {
   MixedLayout m;
   m.base = make_layout<double>(n, nl, nr);
   const size_t mat = m.base.mat;
-  m.smem = pf::NSM_M * mat * 16 + 32 * sizeof(double) + 2 * (size_t)m.base.m * 16 + (size_t)m.base.m * sizeof(int) +
-           64 * sizeof(int);
+  const size_t tail = 32 * sizeof(double) + 2 * (size_t)m.base.m * 16 + (size_t)m.base.m * sizeof(int) +
+                      64 * sizeof(int);
+  m.smem = pf::NSM_M * mat * 16 + tail;
+  m.smem_leads = pf::NSM * mat * 16 + tail;
   const size_t nslab = (size_t)(L + 2);
   m.per_cta = ((size_t)pf::NGM * mat * 16 + nslab * mat * (8 + 8 + 16) + mat * 8 + 255) & ~(size_t)255;
   const size_t c[8] = {(size_t)nq * nl * nl, (size_t)nq * nl * nl, (size_t)nq * nr * nr, (size_t)nq * nr * nr,
@@ -451,8 +454,8 @@ __global__ void __launch_bounds__(kThreads) leads_kernel(pf::MSys sys, pf::Point
   pf::MCtx c;
   const size_t mat = lay.base.mat;
   dcx* s = reinterpret_cast<dcx*>(smem_raw);
-  for (int i = 0; i < pf::NSM_M; ++i) c.sm[i] = s + i * mat;
-  unsigned char* tail = reinterpret_cast<unsigned char*>(s + pf::NSM_M * mat);
+  for (int i = 0; i < pf::NSM_M; ++i) c.sm[i] = i < pf::NSM ? s + i * mat : nullptr;
+  unsigned char* tail = reinterpret_cast<unsigned char*>(s + pf::NSM * mat);
   c.red = reinterpret_cast<double*>(tail);
   c.iwd.rowk = reinterpret_cast<dcx*>(tail + 32 * sizeof(double));
   c.iwd.colk = c.iwd.rowk + lay.base.m;
@@ -783,9 +786,10 @@ size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 template <int S>
 int leads_grid(const MixedLayout& lay, int npts) {
   auto k = leads_kernel<S>;
-  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.smem) != cudaSuccess) return -1;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.smem_leads) != cudaSuccess)
+    return -1;
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, lay.smem) != cudaSuccess) return -1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, lay.smem_leads) != cudaSuccess) return -1;
   if (per_sm < 1) return -1;
   DevInfo d = device_info();
   int g = d.sms * per_sm;
@@ -1195,7 +1199,7 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq, const doubl
     sl.lu = reinterpret_cast<fcx*>(w + plan.off_slabs);
     sl.yv = sl.lu + np * (L + 2) * Bn;
     sl.xv = reinterpret_cast<dcx*>(sl.yv + np * (L + 2) * Bn);
-    leads_kernel<1><<<plan.grid_a, kThreads, lay.smem, st>>>(sys, pts, P, out, lay, plan.per_cta_a, scratch, lo,
+    leads_kernel<1><<<plan.grid_a, kThreads, lay.smem_leads, st>>>(sys, pts, P, out, lay, plan.per_cta_a, scratch, lo,
                                                               lstat, queue);
     PF_CUDA(cudaGetLastError());
     // factorisation + back substitution, then each refinement sweep as a
