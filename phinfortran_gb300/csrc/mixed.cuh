@@ -32,12 +32,16 @@ using fcx = cx<float>;
 // and FP32 copies (factorisation and corrections), same layout as the
 // FP64 input (column-major, ld = rows).
 // Row-compressed (ELL) copy of a block family: row r of block b keeps up to
-// K (column, value) pairs at [(b*rows + r)*K + k]; column -1 ends the row.
+// K (column, value) pairs at [(b*K + k)*rows + r] (slot-major, so the rows a
+// warp reads at one slot are contiguous); column -1 ends the row.
 struct Ell {
   const int* col;
   const dcx* val;
   int K, rows;
 };
+__host__ __device__ __forceinline__ size_t ell_at(size_t blk, int K, int rows, int r, int k) {
+  return (blk * K + k) * (size_t)rows + r;
+}
 
 enum { PF_ELL_K = 16 };
 
@@ -263,11 +267,11 @@ __device__ int mixed_factor_solve(const MCtx& mc, const MSys& sys, int q, fcx zD
 
 // Accumulate acc += M(r,:) X(:,c) over the ELL row of M.
 __device__ __forceinline__ dcx ell_row_dot(const Ell& e, size_t blk, int r, const dcx* X, int ld, int c, dcx acc) {
-  const size_t base = (blk * e.rows + r) * (size_t)e.K;
   for (int k = 0; k < e.K; ++k) {
-    const int cc = e.col[base + k];
+    const size_t at = ell_at(blk, e.K, e.rows, r, k);
+    const int cc = e.col[at];
     if (cc < 0) break;
-    acc = cfma(e.val[base + k], X[cc + c * ld], acc);
+    acc = cfma(e.val[at], X[cc + c * ld], acc);
   }
   return acc;
 }

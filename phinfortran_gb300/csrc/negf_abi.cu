@@ -292,14 +292,15 @@ __global__ void build_ell_kernel(const dcx* M, int rows, int cols, int count, in
       const bool nz = v.x.hi != 0.f || v.x.lo != 0.f || v.y.hi != 0.f || v.y.lo != 0.f;
       if (!nz) continue;
       if (k < K) {
-        col_out[t * K + k] = c;
-        val_out[t * K + k] = v;
+        const size_t at = pf::ell_at(b, K, orows, r, k);
+        col_out[at] = c;
+        val_out[at] = v;
       } else {
         atomicOr(overflow, 1);
       }
       ++k;
     }
-    for (; k < K; ++k) col_out[t * K + k] = -1;
+    for (; k < K; ++k) col_out[pf::ell_at(b, K, orows, r, k)] = -1;
   }
 }
 
@@ -505,26 +506,51 @@ __global__ void __launch_bounds__(kThreads) leads_kernel(pf::MSys sys, pf::Point
 }
 
 
-// Refinement residual of every point and every extended layer in parallel:
-// r_j = b_j - A X (df64), written in FP32 into the forward-vector slab
-// (the forward pass consumes r_j before it overwrites the slot with y_j).
-// One thread per element; lanes run along the rows of one column.
-__device__ __forceinline__ dcx ell_acc(const pf::Ell& e, size_t blk, int r, const dcx* X, int c, dcx acc) {
-  const size_t base = (blk * e.rows + r) * (size_t)e.K;
-  for (int k = 0; k < e.K; ++k) {
-    const int cc = e.col[base + k];
-    if (cc < 0) break;
-    acc = pf::cfma(e.val[base + k], X[cc + c * pf::wp::NW], acc);
-  }
-  return acc;
+// Refinement residual r_j = b_j - A X (df64) of every point and every
+// extended layer, written in FP32 into the forward-vector slab (the forward
+// pass consumes r_j before it overwrites the slot with y_j).
+//
+// One CTA of kResThreads threads takes a run of kResLayers consecutive
+// layers of one point.  The solution blocks X_{j-1}, X_j, X_{j+1} sit in a
+// four-slot window of shared memory (X_j in slot j % 4); X_{j+2} is fetched
+// into registers before layer j is computed and stored after it, so its
+// global latency overlaps the arithmetic.  Thread (r, c0) computes row r of
+// columns c0, c0 + 8, c0 + 16, c0 + 24: every ELL (or dense) entry of row r
+// feeds four independent accumulators.
+constexpr int kResThreads = 256;
+constexpr int kResLayers = 8;
+constexpr int kResCols = pf::wp::NW * pf::wp::NW / kResThreads;  // columns a thread
+constexpr int kResColStep = kResThreads / pf::wp::NW;              // column stride
+constexpr size_t kResSmem = 4 * (size_t)pf::wp::NW * pf::wp::NW * sizeof(dcx);
+
+__device__ __forceinline__ void res_fetch(dcx (&v)[kResCols], const dcx* src) {
+#pragma unroll
+  for (int i = 0; i < kResCols; ++i) v[i] = src[threadIdx.x + i * kResThreads];
 }
-__device__ __forceinline__ dcx dense_acc(const dcx* M, int ldm, int kdim, bool ct, int r, const dcx* X, int c,
-                                         dcx acc) {
+__device__ __forceinline__ void res_put(dcx* dst, const dcx (&v)[kResCols]) {
+#pragma unroll
+  for (int i = 0; i < kResCols; ++i) dst[threadIdx.x + i * kResThreads] = v[i];
+}
+// acc[i] += M(r, :) X(:, c0 + i*kResColStep) over the ELL row r of block blk
+__device__ __forceinline__ void ell_acc4(const pf::Ell& e, size_t blk, int r, const dcx* X, int c0,
+                                         dcx (&acc)[kResCols]) {
+  for (int k = 0; k < e.K; ++k) {
+    const size_t at = pf::ell_at(blk, e.K, e.rows, r, k);
+    const int cc = e.col[at];
+    if (cc < 0) break;
+    const dcx v = e.val[at];
+#pragma unroll
+    for (int i = 0; i < kResCols; ++i) acc[i] = pf::cfma(v, X[cc + (c0 + i * kResColStep) * pf::wp::NW], acc[i]);
+  }
+}
+// the same with a dense (ct: conjugate-transposed) global block
+__device__ __forceinline__ void dense_acc4(const dcx* M, int ldm, int kdim, bool ct, int r, const dcx* X, int c0,
+                                           dcx (&acc)[kResCols]) {
   for (int k = 0; k < kdim; ++k) {
     const dcx m = ct ? pf::cconj(M[k + (size_t)r * ldm]) : M[r + (size_t)k * ldm];
-    acc = pf::cfma(m, X[k + c * pf::wp::NW], acc);
+#pragma unroll
+    for (int i = 0; i < kResCols; ++i) acc[i] = pf::cfma(m, X[k + (c0 + i * kResColStep) * pf::wp::NW], acc[i]);
   }
-  return acc;
 }
 
 // Per-point energies in df64: zL = E + i eps, zD = E + i dev_factor eps.
@@ -537,59 +563,94 @@ __global__ void point_z_kernel(pf::Points pts, pf::Params P, dcx* z2) {
   z2[2 * p + 1] = pf::mk<pf::df64>(pf::df64(E), pf::df64(P.dev_factor * eps));
 }
 
-__global__ void residual_kernel(pf::MSys s, pf::Points pts, const dcx* z2, pf::wp::LeadOut lo, pf::wp::Slabs sl) {
-  const int NW = pf::wp::NW;
-  const size_t B = (size_t)NW * NW;
-  const int L = s.L, n = s.n;
-  const size_t per_pt = (size_t)(L + 2) * B;
-  const size_t total = (size_t)pts.npts * per_pt;
+__global__ void __launch_bounds__(kResThreads)
+    residual_kernel(pf::MSys s, pf::Points pts, const dcx* z2, pf::wp::LeadOut lo, pf::wp::Slabs sl) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  dcx* win = reinterpret_cast<dcx*>(smem_raw);
+  constexpr int NW = pf::wp::NW;
+  constexpr int B = NW * NW;
+  const int L = s.L, n = s.n, nb = L + 2;
+  const int r = threadIdx.x % NW, c0 = threadIdx.x / NW;
+  const int runs = (nb + kResLayers - 1) / kResLayers;
   const bool sparse = s.ell_overflow != nullptr && *s.ell_overflow == 0;
-  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (size_t)gridDim.x * blockDim.x) {
-    const int r = (int)(idx % NW);
-    const int c = (int)((idx / NW) % NW);
-    const int j = (int)((idx / B) % (L + 2));
-    const int p = (int)(idx / per_pt);
-    const int dj = j == 0 ? s.nl : (j == L + 1 ? s.nr : n);
-    fcx outv = pf::mk<float>(0.f, 0.f);
-    if (r < dj && c < s.nr) {
-      const int q = pts.qidx ? pts.qidx[p] : 0;
-      const dcx z = z2[2 * p + (j == 0 ? 0 : 1)];
-      const dcx* xb = sl.xv + (size_t)p * per_pt;
-      const dcx* X0 = xb + (size_t)j * B;
-      dcx acc = pf::csub(pf::wp::dz(), pf::cmul(z, X0[r + c * NW]));
-      if (j == L + 1 && r == c) acc.x = acc.x + pf::df64(1.f, 0.f);
-      if (j == 0) {
-        acc = dense_acc(lo.esl + (size_t)p * B, NW, s.nl, false, r, X0, c, acc);
-        const dcx* Xp = xb + B;
-        acc = sparse ? ell_acc(s.eHld, (size_t)q, r, Xp, c, acc)
-                     : dense_acc(s.Hld + (size_t)q * s.nl * n, s.nl, n, false, r, Xp, c, acc);
-      } else if (j <= L) {
-        const dcx* Xm = xb + (size_t)(j - 1) * B;
-        const dcx* Xp = xb + (size_t)(j + 1) * B;
-        if (sparse) {
-          acc = ell_acc(s.eHd, (size_t)q * L + (j - 1), r, X0, c, acc);
-          acc = (j == 1) ? ell_acc(s.eHldH, (size_t)q, r, Xm, c, acc)
-                         : ell_acc(s.eHdvH, (size_t)q * (L - 1) + (j - 2), r, Xm, c, acc);
-          acc = (j == L) ? ell_acc(s.eHrdH, (size_t)q, r, Xp, c, acc)
-                         : ell_acc(s.eHdv, (size_t)q * (L - 1) + (j - 1), r, Xp, c, acc);
-        } else {
-          acc = dense_acc(s.Hd + ((size_t)q * L + (j - 1)) * n * n, n, n, false, r, X0, c, acc);
-          acc = (j == 1) ? dense_acc(s.Hld + (size_t)q * s.nl * n, s.nl, s.nl, true, r, Xm, c, acc)
-                         : dense_acc(s.Hdv + ((size_t)q * (L - 1) + (j - 2)) * n * n, n, n, true, r, Xm, c, acc);
-          acc = (j == L) ? dense_acc(s.Hrd + (size_t)q * s.nr * n, s.nr, s.nr, true, r, Xp, c, acc)
-                         : dense_acc(s.Hdv + ((size_t)q * (L - 1) + (j - 1)) * n * n, n, n, false, r, Xp, c, acc);
-        }
-      } else {
-        const dcx* Xm = xb + (size_t)L * B;
-        acc = dense_acc(s.HR + (size_t)q * s.nr * s.nr, s.nr, s.nr, false, r, X0, c, acc);
-        acc = dense_acc(lo.sr + (size_t)p * B, NW, s.nr, false, r, X0, c, acc);
-        acc = sparse ? ell_acc(s.eHrd, (size_t)q, r, Xm, c, acc)
-                     : dense_acc(s.Hrd + (size_t)q * s.nr * n, s.nr, n, false, r, Xm, c, acc);
-      }
-      outv = pf::mk<float>(acc.x.hi, acc.y.hi);
+  for (int task = blockIdx.x; task < pts.npts * runs; task += gridDim.x) {
+    const int p = task / runs;
+    const int j0 = (task % runs) * kResLayers;
+    const int j1 = j0 + kResLayers < nb ? j0 + kResLayers : nb;
+    const int q = pts.qidx ? pts.qidx[p] : 0;
+    const dcx* xb = sl.xv + (size_t)p * nb * B;
+    fcx* yb = sl.yv + (size_t)p * nb * B;
+    dcx nxt[kResCols];
+    __syncthreads();  // the previous run is done with the window
+    for (int jj = (j0 > 0 ? j0 - 1 : 0); jj <= j0 + 1 && jj < nb; ++jj) {
+      res_fetch(nxt, xb + (size_t)jj * B);
+      res_put(win + (jj & 3) * B, nxt);
     }
-    sl.yv[idx] = outv;
+    __syncthreads();
+    for (int j = j0; j < j1; ++j) {
+      const bool more = j + 1 < j1 && j + 2 < nb;  // layer j+1 of this run needs X_{j+2}
+      if (more) res_fetch(nxt, xb + (size_t)(j + 2) * B);
+      const int dj = j == 0 ? s.nl : (j == L + 1 ? s.nr : n);
+      const dcx* X0 = win + (j & 3) * B;
+      const dcx* Xm = win + ((j + 3) & 3) * B;
+      const dcx* Xp = win + ((j + 1) & 3) * B;
+      fcx outv[kResCols];
+#pragma unroll
+      for (int i = 0; i < kResCols; ++i) outv[i] = pf::mk<float>(0.f, 0.f);
+      if (r < dj) {
+        const dcx z = z2[2 * p + (j == 0 ? 0 : 1)];
+        dcx acc[kResCols];
+#pragma unroll
+        for (int i = 0; i < kResCols; ++i) {
+          const int c = c0 + i * kResColStep;
+          acc[i] = pf::csub(pf::wp::dz(), pf::cmul(z, X0[r + c * NW]));
+          if (j == L + 1 && r == c) acc[i].x = acc[i].x + pf::df64(1.f, 0.f);
+        }
+        if (j == 0) {
+          dense_acc4(lo.esl + (size_t)p * B, NW, s.nl, false, r, X0, c0, acc);
+          if (sparse)
+            ell_acc4(s.eHld, (size_t)q, r, Xp, c0, acc);
+          else
+            dense_acc4(s.Hld + (size_t)q * s.nl * n, s.nl, n, false, r, Xp, c0, acc);
+        } else if (j <= L) {
+          if (sparse) {
+            ell_acc4(s.eHd, (size_t)q * L + (j - 1), r, X0, c0, acc);
+            if (j == 1)
+              ell_acc4(s.eHldH, (size_t)q, r, Xm, c0, acc);
+            else
+              ell_acc4(s.eHdvH, (size_t)q * (L - 1) + (j - 2), r, Xm, c0, acc);
+            if (j == L)
+              ell_acc4(s.eHrdH, (size_t)q, r, Xp, c0, acc);
+            else
+              ell_acc4(s.eHdv, (size_t)q * (L - 1) + (j - 1), r, Xp, c0, acc);
+          } else {
+            dense_acc4(s.Hd + ((size_t)q * L + (j - 1)) * n * n, n, n, false, r, X0, c0, acc);
+            if (j == 1)
+              dense_acc4(s.Hld + (size_t)q * s.nl * n, s.nl, s.nl, true, r, Xm, c0, acc);
+            else
+              dense_acc4(s.Hdv + ((size_t)q * (L - 1) + (j - 2)) * n * n, n, n, true, r, Xm, c0, acc);
+            if (j == L)
+              dense_acc4(s.Hrd + (size_t)q * s.nr * n, s.nr, s.nr, true, r, Xp, c0, acc);
+            else
+              dense_acc4(s.Hdv + ((size_t)q * (L - 1) + (j - 1)) * n * n, n, n, false, r, Xp, c0, acc);
+          }
+        } else {
+          dense_acc4(s.HR + (size_t)q * s.nr * s.nr, s.nr, s.nr, false, r, X0, c0, acc);
+          dense_acc4(lo.sr + (size_t)p * B, NW, s.nr, false, r, X0, c0, acc);
+          if (sparse)
+            ell_acc4(s.eHrd, (size_t)q, r, Xm, c0, acc);
+          else
+            dense_acc4(s.Hrd + (size_t)q * s.nr * n, s.nr, n, false, r, Xm, c0, acc);
+        }
+#pragma unroll
+        for (int i = 0; i < kResCols; ++i)
+          if (c0 + i * kResColStep < s.nr) outv[i] = pf::mk<float>(acc[i].x.hi, acc[i].y.hi);
+      }
+#pragma unroll
+      for (int i = 0; i < kResCols; ++i) yb[(size_t)j * B + r + (c0 + i * kResColStep) * NW] = outv[i];
+      if (more) res_put(win + ((j + 2) & 3) * B, nxt);
+      __syncthreads();
+    }
   }
 }
 
@@ -776,6 +837,7 @@ struct MixedPlan {
   MixedLayout lay;
   bool warp_engine;     // cross-sections <= 32: leads kernel + warp-per-point layer kernel
   int grid_a, grid_b;   // CTA counts of the (leads / fused) kernel and the layer kernel
+  int grid_r;           // resident CTAs of the residual kernel
   size_t per_cta_a;     // per-CTA scratch of kernel A
   size_t off_blocks, off_ell, off_scratch, off_lead, off_lstat, off_z, off_slabs, total;
   size_t smem_b;
@@ -820,10 +882,20 @@ bool make_plan(int n, int nl, int nr, int L, int nq, int npts, MixedPlan& P) {
     int gb = d.sms * per_sm;
     const int need_ctas = (warps + kWarpsPerCta - 1) / kWarpsPerCta;
     P.grid_b = gb < need_ctas ? gb : need_ctas;
+    if (cudaFuncSetAttribute(residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kResSmem) !=
+        cudaSuccess)
+      return false;
+    int per_sm_r = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_r, residual_kernel, kResThreads, kResSmem) !=
+            cudaSuccess ||
+        per_sm_r < 1)
+      return false;
+    P.grid_r = d.sms * per_sm_r;
   } else {
     P.grid_a = (S == 1) ? mixed_grid<1>(lay, np) : mixed_grid<2>(lay, np);
     P.per_cta_a = lay.per_cta;
     P.grid_b = 0;
+    P.grid_r = 0;
     P.smem_b = 0;
   }
   if (P.grid_a <= 0) return false;
@@ -1207,12 +1279,12 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq, const doubl
     // then the Caroli trace
     layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 0, out, lo, sl, lstat, queue_b);
     PF_CUDA(cudaGetLastError());
-    const size_t rtotal = (size_t)npts * (L + 2) * Bn;
-    const int rblocks = (int)((rtotal + 255) / 256 < (size_t)d.sms * 16 ? (rtotal + 255) / 256 : (size_t)d.sms * 16);
+    const long rtasks = (long)npts * ((L + 2 + kResLayers - 1) / kResLayers);
+    const int rblocks = (int)(rtasks < (long)plan.grid_r ? rtasks : (long)plan.grid_r);
     dcx* z2 = reinterpret_cast<dcx*>(w + plan.off_z);
     if (refine_iters > 0) point_z_kernel<<<(npts + 127) / 128, 128, 0, st>>>(pts, P, z2);
     for (int it = 0; it < refine_iters; ++it) {
-      residual_kernel<<<rblocks, 256, 0, st>>>(sys, pts, z2, lo, sl);
+      residual_kernel<<<rblocks, kResThreads, kResSmem, st>>>(sys, pts, z2, lo, sl);
       PF_CUDA(cudaMemsetAsync(queue_b, 0, sizeof(int), st));
       layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 1, out, lo, sl, lstat,
                                                                          queue_b);
