@@ -155,11 +155,14 @@ __device__ __forceinline__ void stage_rows(fcx* S, const GView& g, int lane) {
 // In-place Gauss-Jordan inverse of the 32x32 matrix in S with implicit
 // partial pivoting (pivot = first max |re|+|im| among unused rows), then
 // the unscrambled inverse is written to D (smem) and optionally to global
-// (ld 32).  Returns status bits (uniform).
+// (ld 32).  Lane r owns row r, so every shared access is either a row-r
+// element (consecutive lanes, conflict free) or a broadcast of the pivot
+// row.  Returns status bits (uniform).
 __device__ int winverse(fcx* S, fcx* D, fcx* gout, int lane) {
   unsigned used = 0u;
   int status = PF_OK;
-  int perm_mine = 0;  // P[lane]
+  int perm_mine = 0;  // P[lane]: pivot row of step `lane`
+  int step_mine = 0;  // the step whose pivot row was `lane`
   for (int k = 0; k < NW; ++k) {
     const fcx mk_ = S[lane + k * LDW];
     float v = fabsf(mk_.x) + fabsf(mk_.y);
@@ -178,38 +181,37 @@ __device__ int winverse(fcx* S, fcx* D, fcx* gout, int lane) {
     }
     const int p = bi;
     if (lane == k) perm_mine = p;
-    const fcx piv = S[p + k * LDW];
+    if (lane == p) step_mine = k;
+    const fcx piv = mk<float>(__shfl_sync(0xffffffffu, mk_.x, p), __shfl_sync(0xffffffffu, mk_.y, p));
     if (piv.x == 0.f && piv.y == 0.f) status |= PF_SINGULAR;
     if (!(isfinite(piv.x) && isfinite(piv.y))) status |= PF_NAN;
     const fcx ip = crecip(piv);
-    fcx colk[NW];
+    fcx rowp[NW];
 #pragma unroll
-    for (int r = 0; r < NW; ++r) colk[r] = S[r + k * LDW];
-    const fcx rowp = S[p + lane * LDW];
+    for (int c = 0; c < NW; ++c) rowp[c] = S[p + c * LDW];
     __syncwarp();
-    // column k becomes -col_k / piv (ip on the pivot row), every other
-    // column c becomes col_c - col_k f_c with f_c = S(p, c) / piv: one
-    // update for all lanes, with (old, f) = (0, ip) on lane k
-    const bool pivcol = lane == k;
-    const fcx f = pivcol ? ip : cmul(rowp, ip);
+    // row r != p becomes row_r - m_r row_p with m_r = S(r, k) / piv, and
+    // column k becomes -m; the pivot row becomes row_p / piv, i.e. the same
+    // update from a zero row with m = -1/piv (column k: 1/piv)
+    const bool prow = lane == p;
+    const fcx m = prow ? mk<float>(-ip.x, -ip.y) : cmul(mk_, ip);
 #pragma unroll
-    for (int r = 0; r < NW; ++r) {
-      const fcx old = pivcol ? fz() : S[r + lane * LDW];
-      const fcx nv = mk<float>(old.x - (colk[r].x * f.x - colk[r].y * f.y),
-                               old.y - (colk[r].x * f.y + colk[r].y * f.x));
-      S[r + lane * LDW] = (r == p) ? f : nv;
+    for (int c = 0; c < NW; ++c) {
+      const fcx old = prow ? fz() : S[lane + c * LDW];
+      const fcx nv = mk<float>(old.x - (m.x * rowp[c].x - m.y * rowp[c].y),
+                               old.y - (m.x * rowp[c].y + m.y * rowp[c].x));
+      S[lane + c * LDW] = (c == k) ? mk<float>(-m.x, -m.y) : nv;
     }
     used |= 1u << p;
     __syncwarp();
   }
-  // inv[k, P[c]] = M[P[k], c]: lane c moves its column to column P[c]
-  const int pc = perm_mine;  // lane c holds P[c]
+  // inv[k, P[j]] = M[P[k], j]: lane r = P[k] moves its row to row k
 #pragma unroll
-  for (int k = 0; k < NW; ++k) {
-    const int pk = __shfl_sync(0xffffffffu, perm_mine, k);
-    const fcx e = S[pk + lane * LDW];
-    D[k + pc * LDW] = e;
-    if (gout) gout[k + pc * NW] = e;
+  for (int j = 0; j < NW; ++j) {
+    const int pj = __shfl_sync(0xffffffffu, perm_mine, j);
+    const fcx e = S[lane + j * LDW];
+    D[step_mine + pj * LDW] = e;
+    if (gout) gout[step_mine + pj * NW] = e;
   }
   __syncwarp();
   return status;
