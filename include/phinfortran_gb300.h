@@ -395,6 +395,73 @@ int pf_tb_hk_blocks(int natoms, const double* pos, const int* species,
 /* Message for the last error of pf_tb_hk_blocks. */
 const char* pf_tb_last_error(void);
 
+/* ---------------------------------------------------------------------------
+ * Binary force-constant (full-Hamiltonian) phonon path.
+ *
+ * pf_gen_dyn replaces gen_dyn_mpi (negf/dyn.f90:7-37 -> gen_dyn :39-150) and,
+ * called with the lead tables and nz = 1, gen_dyn_lead_mpi
+ * (negf/dyn.f90:152-187 -> gen_dyn_lead :190-312): the dense norb x norb
+ * dynamical matrix, norb = 3 natoms, in THz^2,
+ *   D(a i, b j) = sum over the entries of (a, b) of
+ *                 fc(3 r(a) + i, 3 idx + j) exp(i dr . k) / sqrt(m_a m_b)
+ * Hermitised (0.5 (D + D^H)) when `hermitize` is nonzero (gen_dyn, and the
+ * in-layer matrix of gen_dyn_lead; its coupling matrix is not).  The entries
+ * are the reference's reduced tables as the driver holds them
+ * (negf/phinfortran.f90:655-683):
+ *   num_mat[natoms x natoms]     Fortran column-major, num_mat(a+1, b+1) at
+ *                                a + b*natoms; the entries run over (a, b)
+ *                                row-major as the reference flattens them
+ *   idx_mat_red[nent]            1-based fc column atoms
+ *   dist_mat_red[nent x 3]       column-major (component c of entry e at
+ *                                e + c*nent), Angstrom
+ *   force_constant[fc_rows x fc_cols] column-major, eV/A^2, fc_rows = 3 n_uc
+ *   mass[natoms]                 amu (mass_no of each atom's species)
+ *   recivec[3][3]                rows = reciprocal vectors, kpoints[nq][3]
+ *                                fractional (k = kpoint . recivec)
+ * Atom a's fc row atom follows the z-slice order of negf/dyn.f90:95-103
+ * (natoms = nbx*nby*n_uc, n_uc a multiple of nz).  Ham receives nq
+ * column-major complex matrices.  Host pointers; synchronous.
+ */
+int pf_gen_dyn(int natoms, int nbx, int nby, int n_uc, int nz, int fc_rows,
+               int fc_cols, const double* force_constant, const int* num_mat,
+               int nent, const int* idx_mat_red, const double* dist_mat_red,
+               const double* mass, const double* recivec, int nq,
+               const double* kpoints, int hermitize, double* Ham);
+
+/* The same on device buffers with the tables already packed: npairs atom
+ * pairs (pair_a, pair_b 0-based) whose entries are pair_off[p] ..
+ * pair_off[p+1]-1 of ent_idx (0-based fc column atom) and ent_dr[nent][3];
+ * row_atom[natoms] the fc row atom of each atom, kcart[nq][3] Cartesian.
+ * H receives nq column-major norb x norb complex matrices.  Asynchronous on
+ * `stream`. */
+int pf_gen_dyn_dev(int natoms, int fc_rows, const double* force_constant,
+                   int npairs, const int* pair_a, const int* pair_b,
+                   const int* pair_off, const int* ent_idx,
+                   const double* ent_dr, const int* row_atom,
+                   const double* mass, int nq, const double* kcart,
+                   int hermitize, double* H, cudaStream_t stream);
+
+/* Block set of the tdb transport entries taken from nq dense matrices
+ * (column-major norb x norb complex, device) as the full-Hamiltonian path
+ * slices them: the left lead cell next to the device at rows n_buffer_l+nl
+ * .. n_buffer_l+2nl-1 (Haml, and Hamlv = the block from the outer cell),
+ * negf/surface.f90:170-198; the device layers from layer_start (device
+ * int[L+1], orbital offsets from n_buffer_l+2nl; negf/device.f90:323-500,
+ * the partition of blockwise_setup, :11-249); the right cells mirrored.
+ * Every device block is zero-padded to n x n (padding rows/columns of the
+ * couplings are zero, so the transmission is unchanged).  Outputs are the
+ * device arrays of pf_transport_tdb_dev with a leading k axis.  *bad (device)
+ * is set when a slice leaves the matrix.  Asynchronous on `stream`. */
+int pf_dense_to_tdb_dev(int norb, int nq, const double* H, int nl, int nr,
+                        int n_buffer_l, int n_buffer_r, int L,
+                        const int* layer_start, int n, double* HL,
+                        double* HLv, double* HR, double* HRv, double* Hd,
+                        double* Hdv, double* Hld, double* Hrd, int* bad,
+                        cudaStream_t stream);
+
+/* Message for the last error of the full-Hamiltonian entries. */
+const char* pf_fullh_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,6 +89,12 @@ SIGNATURES = {
                                              C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
                                              C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_size_t, C.c_void_p]),
+    "pf_fullh_last_error": (C.c_char_p, []),
+    "pf_gen_dyn": (C.c_int, [C.c_int] * 7 + [_dp, _ip, C.c_int, _ip, _dp, _dp, _dp, C.c_int, _dp, C.c_int, _dp]),
+    "pf_gen_dyn_dev": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_int] + [C.c_void_p] * 7
+                       + [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "pf_dense_to_tdb_dev": (C.c_int, [C.c_int, C.c_int, C.c_void_p] + [C.c_int] * 5 + [C.c_void_p, C.c_int]
+                            + [C.c_void_p] * 10),
     "pf_tb_last_error": (C.c_char_p, []),
     "pf_tb_hk_blocks": (C.c_int, [C.c_int, _dp, _ip, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp, C.c_double,
                                   C.c_int, _dp, C.c_int, _ip, _dp]),

@@ -303,3 +303,110 @@ def tb_ribbon3(W=256, L=1000, norb=3, onsite_sigma=0.3, hop_spread=0.1, ne=4096,
         E = E[np.asarray(energies)]
     params = dict(eta=0.0, eta0=eta, dev_factor=1.0, convergence=convergence)
     return blocks, E, params
+
+
+# THz^2 per (eV/A^2 / amu): the unit factor of negf/dyn.f90:138
+FC_TO_THZ2 = 1.609e-19 / 1.0e-20 / 1.6726219e-27 / (1.0e12 * 2.0 * 3.141592653589793238) ** 2
+
+
+def sc_bar_binary_fc(nx=2, ny=2, L=6, a0=2.0, k=1.0, mass_range=(20.0, 40.0), lead_mass=28.0,
+                     bond_range=(0.8, 1.2), seed_index=4):
+    """The simple-cubic bar of ``sc_phonon`` (per-atom masses, per-bond
+    springs in the device) written as the input of the binary
+    force-constant path: the whole sandwich (L + 6 layers, ScBar layout) is
+    one unit cell, periodic transversally (nx x ny) and along z, with one
+    species per atom; fc (3 n_uc, 27 * 3 n_uc) in eV/A^2 holds -k e e^T
+    for every bond to the neighbour's supercell image and the matching self
+    terms (acoustic sum rule).  Springs in eV/A^2, masses in amu, positions
+    in Angstrom (lattice constant a0).  Returns a dict with the arrays the
+    reference holds (fc, positions, supercell positions, cells, masses,
+    sizes) and ``bar_blocks``: the ScBar blocks of the same model in THz^2,
+    which the full-Hamiltonian path must reproduce at k = 0."""
+    rng = _rng(seed_index)
+    bar = ScBar(nx, ny, L)
+    nc, nlay = bar.nc, bar.nlay
+    n_uc = nc * nlay
+    masses = np.full(n_uc, float(lead_mass))
+    masses[bar.dev_atoms] = rng.uniform(*mass_range, size=bar.dev_atoms.size)
+    springs = np.full(len(bar.bonds), float(k))
+    springs[bar.dev_bond] = rng.uniform(*bond_range, size=int(bar.dev_bond.sum())) * k
+    idx = np.arange(n_uc)
+    ix, iy, iz = idx % nx, (idx // nx) % ny, idx // nc
+    pos = np.stack([ix * a0, iy * a0, iz * a0, idx + 1.0], axis=1)       # column 4: species (1-based)
+    cell = np.diag([nx * a0, ny * a0, nlay * a0]).astype(np.float64)
+    recivec = np.ascontiguousarray((2.0 * np.pi * np.linalg.inv(cell)).T)
+
+    def sc(off, atom):   # fc supercell column atom (nfc = (1, 1, 1)), negf/input.f90:462-463
+        return ((off[0] + 1) * 9 + (off[1] + 1) * 3 + 1 + off[2]) * n_uc + atom
+
+    fc = np.zeros((3 * n_uc, 27 * 3 * n_uc))
+    for (a, b, axis), s in zip(bar.bonds, springs):
+        off = [0, 0, 0]
+        if axis == 0 and ix[b] < ix[a]:
+            off[0] = 1
+        if axis == 1 and iy[b] < iy[a]:
+            off[1] = 1
+        neg = [-o for o in off]
+        fc[3 * a + axis, 3 * sc(off, b) + axis] -= s
+        fc[3 * b + axis, 3 * sc(neg, a) + axis] -= s
+        fc[3 * a + axis, 3 * sc([0, 0, 0], a) + axis] += s
+        fc[3 * b + axis, 3 * sc([0, 0, 0], b) + axis] += s
+    pos_sc = np.zeros((27 * n_uc, 4))
+    for i in (-1, 0, 1):
+        for j in (-1, 0, 1):
+            for kk in (-1, 0, 1):
+                base = sc([i, j, kk], 0)
+                pos_sc[base:base + n_uc, 0:3] = pos[:, 0:3] + np.array([i, j, kk], dtype=np.float64) @ cell
+                pos_sc[base:base + n_uc, 3] = pos[:, 3]
+    blocks = {key: v * FC_TO_THZ2 for key, v in bar.blocks(masses, springs).items()}
+    n3 = 3 * nc
+    return dict(fc=fc, pos=pos, pos_uc=pos, pos_sc=pos_sc, cell=cell, latvec_uc=cell, recivec=recivec,
+                masses=masses, nbx=1, nby=1, n_uc=n_uc, nz=nlay, nfc=(1, 1, 1), r_cutoff=1.2 * a0,
+                nl=n3, nr=n3, n_buffer_l=n3, n_buffer_r=n3, bar=bar, springs=springs, bar_blocks=blocks)
+
+
+def sc_lead_binary_fc(nx=2, ny=2, a0=2.0, k=1.0, mass=28.0):
+    """Lead principal layer of ``sc_bar_binary_fc`` as the reference's lead
+    input: one layer (nx x ny atoms) as the unit cell, periodic in x, y and
+    z (period a0), uniform springs k and mass; fc (3 nc, 27 * 3 nc) eV/A^2
+    with the bonds of every atom to its +x, +y, +z neighbours (and their
+    reverses) and the self terms."""
+    nc = nx * ny
+    idx = np.arange(nc)
+    ix, iy = idx % nx, idx // nx
+    pos = np.stack([ix * a0, iy * a0, np.zeros(nc), np.ones(nc)], axis=1)
+    cell = np.diag([nx * a0, ny * a0, a0]).astype(np.float64)
+
+    def sc(off, atom):
+        return ((off[0] + 1) * 9 + (off[1] + 1) * 3 + 1 + off[2]) * nc + atom
+
+    fc = np.zeros((3 * nc, 27 * 3 * nc))
+    for a in range(nc):
+        for axis in range(3):
+            if axis == 0 and nx == 1 or axis == 1 and ny == 1:
+                continue
+            off = [0, 0, 0]
+            if axis == 0:
+                b = iy[a] * nx + (ix[a] + 1) % nx
+                off[0] = 1 if ix[a] + 1 == nx else 0
+            elif axis == 1:
+                b = ((iy[a] + 1) % ny) * nx + ix[a]
+                off[1] = 1 if iy[a] + 1 == ny else 0
+            else:
+                b = a
+                off[2] = 1
+            neg = [-o for o in off]
+            fc[3 * a + axis, 3 * sc(off, b) + axis] -= k
+            fc[3 * b + axis, 3 * sc(neg, a) + axis] -= k
+            fc[3 * a + axis, 3 * sc([0, 0, 0], a) + axis] += k
+            fc[3 * b + axis, 3 * sc([0, 0, 0], b) + axis] += k
+    pos_sc = np.zeros((27 * nc, 4))
+    for i in (-1, 0, 1):
+        for j in (-1, 0, 1):
+            for kk in (-1, 0, 1):
+                base = sc([i, j, kk], 0)
+                pos_sc[base:base + nc, 0:3] = pos[:, 0:3] + np.array([i, j, kk], dtype=np.float64) @ cell
+                pos_sc[base:base + nc, 3] = 1.0
+    recivec = np.ascontiguousarray((2.0 * np.pi * np.linalg.inv(cell)).T)
+    return dict(fc=fc, pos=pos, pos_sc=pos_sc, cell=cell, recivec=recivec, masses=np.full(nc, float(mass)),
+                nbx=1, nby=1, n_uc=nc, nfc=(1, 1, 1), r_cutoff=1.2 * a0)

@@ -182,13 +182,31 @@ class DeviceTransport:
     def __init__(self, blocks, npts_max, *, eta, eta0, convergence, dev_factor=10.0,
                  max_iter=1000, want_transr=False, device="cuda", precision="fp64", refine_iters=1):
         import torch
-        self.torch = torch
-        lib = _abi.load()
         if isinstance(blocks, dict):
             blocks = TdbBlocks.from_dict(blocks)
         nq, (n, nl, nr, L), arrs = blocks.stacked()
-        self.dims = (n, nl, nr, L, nq)
-        self.dev = {k: torch.from_numpy(fortran_block(v).copy()).to(device) for k, v in arrs.items()}
+        dev = {k: torch.from_numpy(fortran_block(v).copy()).to(device) for k, v in arrs.items()}
+        self._setup(dev, (n, nl, nr, L, nq), npts_max, eta=eta, eta0=eta0, convergence=convergence,
+                    dev_factor=dev_factor, max_iter=max_iter, want_transr=want_transr, device=device,
+                    precision=precision, refine_iters=refine_iters)
+
+    @classmethod
+    def from_device(cls, dev, dims, npts_max, **kw):
+        """Blocks already on the device: dev maps the block names to float64
+        buffers in the C ABI's layout ([q][block][col][row] interleaved
+        complex), dims = (n, nl, nr, L, nq)."""
+        obj = cls.__new__(cls)
+        obj._setup(dev, tuple(dims), npts_max, **kw)
+        return obj
+
+    def _setup(self, dev, dims, npts_max, *, eta, eta0, convergence, dev_factor=10.0, max_iter=1000,
+               want_transr=False, device="cuda", precision="fp64", refine_iters=1):
+        import torch
+        self.torch = torch
+        lib = _abi.load()
+        n, nl, nr, L, nq = dims
+        self.dims = dims
+        self.dev = dev
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.precision = precision
