@@ -318,9 +318,15 @@ class FullH:
         torch = self.torch
         H = self.dynamical(kfrac)
         dev, dims = self.blocks(H)
-        if max(dims[0], dims[1], dims[2]) > 48:
-            raise ValueError("device-resident full-H transport needs layers and lead cells of at most 48 orbitals")
         E = np.ascontiguousarray(E, dtype=np.float64)
+        if max(dims[0], dims[1], dims[2]) > 48:
+            # layers above the resident size: the tiled engine through the host entry
+            from .transport import transport_tdb
+            blocks = {k: np.swapaxes(v[..., 0].cpu().numpy() + 1j * v[..., 1].cpu().numpy(), -1, -2)
+                      for k, v in dev.items()}
+            return transport_tdb(E, blocks, eta=eta, eta0=eta0, convergence=convergence, dev_factor=dev_factor,
+                                 qidx=qidx, max_iter=max_iter, want_transr=False, check=False,
+                                 precision=precision)
         tr = DeviceTransport.from_device({k: v.reshape(-1) for k, v in dev.items()}, dims, E.size, eta=eta,
                                          eta0=eta0, convergence=convergence, dev_factor=dev_factor,
                                          max_iter=max_iter, precision=precision, refine_iters=refine_iters,
