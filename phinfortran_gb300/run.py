@@ -5,6 +5,7 @@
     python -m phinfortran_gb300.run ribbon3  --width 256 --layers 1000 --energies 4 --perturb 1e-15
     python -m phinfortran_gb300.run sc       --layers 40 --energies 64 --mode grad --arith df64
     python -m phinfortran_gb300.run sisi     --kpoints 1 --energies 16 --mode modes
+    python -m phinfortran_gb300.run sisi     --kpoints 49 --energies 61 --mode modes --out out/
 
 Modes: ``transport`` (T per point), ``modes`` (T plus the s/ns sums of the
 mode-resolved transmission; si-si fixture only), ``grad`` (adjoint: T and
@@ -62,6 +63,7 @@ def main():
     ap.add_argument("--width", type=int, default=0)
     ap.add_argument("--nc", type=int, default=2)
     ap.add_argument("--perturb", type=float, default=0.0)
+    ap.add_argument("--out", default="", help="sisi: write the reference's ten output tables into this directory")
     a = ap.parse_args()
     import torch
     out = dict(workload=a.workload, mode=a.mode)
@@ -77,8 +79,12 @@ def main():
                                 rd=f["rd"], n_bloch_x=int(f["n_bloch"][0]), n_bloch_y=int(f["n_bloch"][1]),
                                 buffer_left=buf, period_left=per, buffer_right=buf, period_right=per,
                                 nlayer=int(f["nlayer"]), natm_layer=int(f["natm_layer"]))
-        E1 = f["E"][np.linspace(1, 60, a.energies).astype(int)]
+        if a.energies >= f["E"].size:
+            E1 = f["E"]                         # the full grid; T of ie = 1 is zero (reference rule)
+        else:
+            E1 = f["E"][np.linspace(1, 60, a.energies).astype(int)]
         E = np.tile(E1, len(ks))
+        zf = np.tile((np.arange(E1.size) == 0) & (E1.size == f["E"].size), len(ks)).astype(np.int32)
         q = np.repeat(np.arange(len(ks), dtype=np.int32), E1.size)
         p = dict(eta=float(f["eta"]), eta0=float(f["eta0"]), convergence=float(f["convergence"]),
                  dev_factor=float(f["dev_factor"]))
@@ -86,11 +92,18 @@ def main():
         geo = LeadGeometry.from_qe(f["pos_all"], f["cell"], f["cell_all"], nb, buf, per, buf, per)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = transport_tdb_modes(E, blocks, geo, f["kgrid"][ks], qidx=q, lambda_eta=5e-3, a_z_l=f["cell"][2, 2],
+        r = transport_tdb_modes(E, blocks, geo, f["kgrid"][ks], qidx=q, zero_flag=zf, lambda_eta=5e-3,
+                                a_z_l=f["cell"][2, 2],
                                 a_z_r=f["cell"][2, 2], check=False, **p)
         torch.cuda.synchronize()
         out.update(points=int(E.size), seconds=time.perf_counter() - t0, transl=r["transl"].tolist(),
                    transl_s=r["transl_s"].tolist(), status=int(np.bitwise_or.reduce(r["status"])))
+        if a.out:
+            from .modes import SUM_NAMES
+            from .output import write_trans
+            grid = lambda v: np.asarray(v).reshape(len(ks), E1.size).T      # (ne, nk) as the reference
+            write_trans(a.out, E1, grid(r["transl"]), grid(r["transr"]), **{k: grid(r[k]) for k in SUM_NAMES})
+            out["written"] = a.out
         print(json.dumps(out))
         return
     b, E, p, aux = _build(a)

@@ -8,7 +8,9 @@ The fixture holds (a) the processed force constants and supercell of
 examples/negf/si-si (read by the oracle's restatement of negf/fc.f90), and
 (b) the reference's own committed outputs output/trans{l,r}_tot.dat,
 trans{l,r}_{s,ns}.dat and refl{l,r}_{s,ns}.dat (61 omega^2 x 49 k), so the
-GPU tests can check parity on a machine without the reference checkout.
+GPU tests can check parity on a machine without the reference checkout;
+and tests/golden/sisi_output_head.txt, the first rows of those tables
+verbatim, which pin the text format of the output writer.
 """
 from __future__ import annotations
 
@@ -52,5 +54,22 @@ def main(out=os.path.join(HERE, "sisi.npz")):
     print("wrote", out)
 
 
+TABLES = ["transl_s", "transl_ns", "refll_s", "refll_ns", "transr_s", "transr_ns", "reflr_s", "reflr_ns",
+          "transl_tot", "transr_tot"]
+
+
+def text_heads(out=os.path.join(HERE, "sisi_output_head.txt"), nlines=3):
+    """Verbatim first rows of the ten output tables (the text format of
+    negf/write_data.f90:340-497), one '# name' header before each."""
+    with open(out, "w") as f:
+        for name in TABLES:
+            with open(os.path.join(REF, "output", name + ".dat")) as g:
+                rows = [next(g) for _ in range(nlines)]
+            f.write(f"# {name}\n")
+            f.writelines(rows)
+    print("wrote", out)
+
+
 if __name__ == "__main__":
     main()
+    text_heads()
