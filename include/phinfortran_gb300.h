@@ -462,6 +462,38 @@ int pf_dense_to_tdb_dev(int norb, int nq, const double* H, int nl, int nr,
 /* Message for the last error of the full-Hamiltonian entries. */
 const char* pf_fullh_last_error(void);
 
+/* ---------------------------------------------------------------------------
+ * Buttiker probes (buttiker = 1): per point, get_G_full_tdb with the probe
+ * self-energies (negf/lesser.f90:475-680) and get_G_lesser_tdb
+ * (negf/lesser.f90:1199-1503), i.e. the bodies of get_G_full_tdb_mpi +
+ * get_G_lesser_tdb_mpi (negf/phinfortran.f90:1204-1236) for a batch of
+ * points.  Blocks as pf_transport_tdb (host pointers, n, nl, nr <= 48,
+ * L >= 2).  Per point p and layer i (row-major [p][i], complex interleaved
+ * where marked):
+ *   sigw, dsigw [npts][L] complex: sigma_w(i, ie) and dsigma_wdt(i, ie) of
+ *                set_sigma_bp_w (negf/lesser.f90:12-45) at the point's energy
+ *   f, df [npts][L]: bose_einstein / dbosedT (negf/util.f90:987-1013) at
+ *                sqrt(E) and the probe temperatures; fL, fR [npts] the leads'
+ *   first [npts]: nonzero at the zero-frequency point (ie == 1), may be null
+ * Outputs: transl [npts]; flux_i [npts][L], A_sum [npts][L] (Tr A_i),
+ * Gn_i [npts][L] (Tr Gn_i), flux_left, flux_right [npts] (complex, as the
+ * reference's arrays); jac [npts][L][L] complex, jac[p][i][j] = the
+ * reference's jacobian(nn, ie, i, j).  Synchronous. */
+int pf_buttiker_tdb(int n, int nl, int nr, int L, int nq, const double* HL,
+                    const double* HLv, const double* HR, const double* HRv,
+                    const double* Hd, const double* Hdv, const double* Hld,
+                    const double* Hrd, int npts, const double* E,
+                    const int* qidx, const int* first, const double* sigw,
+                    const double* dsigw, const double* f, const double* df,
+                    const double* fL, const double* fR, double eta,
+                    double eta0, double dev_factor, double convergence,
+                    int max_iter, double* transl, double* flux_i, double* jac,
+                    double* A_sum, double* Gn_i, double* flux_left,
+                    double* flux_right, int* status);
+
+/* Message for the last error of pf_buttiker_tdb. */
+const char* pf_buttiker_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -95,6 +95,9 @@ SIGNATURES = {
                        + [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "pf_dense_to_tdb_dev": (C.c_int, [C.c_int, C.c_int, C.c_void_p] + [C.c_int] * 5 + [C.c_void_p, C.c_int]
                             + [C.c_void_p] * 10),
+    "pf_buttiker_last_error": (C.c_char_p, []),
+    "pf_buttiker_tdb": (C.c_int, [C.c_int] * 5 + [_dp] * 8 + [C.c_int, _dp, _ip, _ip] + [_dp] * 6
+                        + [C.c_double] * 4 + [C.c_int] + [_dp] * 7 + [_ip]),
     "pf_tb_last_error": (C.c_char_p, []),
     "pf_tb_hk_blocks": (C.c_int, [C.c_int, _dp, _ip, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp, C.c_double,
                                   C.c_int, _dp, C.c_int, _ip, _dp]),
