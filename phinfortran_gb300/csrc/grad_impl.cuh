@@ -8,7 +8,7 @@ namespace pfgrad {
 
 using pf::cx;
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;  // one CTA per SM (shared memory): 16 warps per point
 
 struct GLayout {
   int m, ld;
