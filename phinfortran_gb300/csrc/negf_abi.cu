@@ -39,6 +39,7 @@ int cuda_err(cudaError_t e, const char* where) {
   } while (0)
 
 constexpr int kThreads = 256;
+constexpr int kMixedThreads = 512;  // fused mixed kernel (blocks above 32): one CTA per SM, 16 warps per point
 
 // Layout of the per-CTA scratch: NG matrices of ld*m elements.
 struct Layout {
@@ -350,7 +351,7 @@ MixedLayout make_mixed_layout(int n, int nl, int nr, int L, int nq) {
 }
 
 template <int S>
-__global__ void __launch_bounds__(kThreads) mixed_kernel(pf::MSys sys, pf::Points pts, pf::Params P, int nref,
+__global__ void __launch_bounds__(kMixedThreads) mixed_kernel(pf::MSys sys, pf::Points pts, pf::Params P, int nref,
                                                          pf::Outputs out, MixedLayout lay, char* scratch,
                                                          int* queue) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -825,7 +826,7 @@ int mixed_grid(const MixedLayout& lay, int npts) {
   auto k = mixed_kernel<S>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.smem) != cudaSuccess) return -1;
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, lay.smem) != cudaSuccess) return -1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kMixedThreads, lay.smem) != cudaSuccess) return -1;
   if (per_sm < 1) return -1;
   DevInfo d = device_info();
   int g = d.sms * per_sm;
@@ -1293,9 +1294,9 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq, const doubl
     PF_CUDA(cudaMemsetAsync(queue_b, 0, sizeof(int), st));
     layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 2, out, lo, sl, lstat, queue_b);
   } else if (S == 1) {
-    mixed_kernel<1><<<plan.grid_a, kThreads, lay.smem, st>>>(sys, pts, P, refine_iters, out, lay, scratch, queue);
+    mixed_kernel<1><<<plan.grid_a, kMixedThreads, lay.smem, st>>>(sys, pts, P, refine_iters, out, lay, scratch, queue);
   } else {
-    mixed_kernel<2><<<plan.grid_a, kThreads, lay.smem, st>>>(sys, pts, P, refine_iters, out, lay, scratch, queue);
+    mixed_kernel<2><<<plan.grid_a, kMixedThreads, lay.smem, st>>>(sys, pts, P, refine_iters, out, lay, scratch, queue);
   }
   PF_CUDA(cudaGetLastError());
   return PF_SUCCESS;
