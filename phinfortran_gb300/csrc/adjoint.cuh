@@ -324,6 +324,9 @@ __device__ int adjoint_point_ckpt(const Ctx<R>& c, const System<R>& sys, int q, 
       st |= ckpt_step<R, S>(c, sys, q, zD, j, sl.segg + (size_t)(i - 1) * mat, sl.segy + (size_t)(i - 1) * mat, s1, s2,
                          sZ, sl.segg + (size_t)i * mat, sl.segy + (size_t)i * mat);
     }
+    // W is the right operand of every K_j of the segment: keep it in the
+    // shared slot the recomputation used as scratch
+    copy_in(s2, ld, opN<R>(sl.W, ld), nr, nl);
     for (int j = e - 1; j >= c0; --j) {
       const int dj = xdim(sys, j);
       const cx<R>* gj = sl.segg + (size_t)(j - c0) * mat;
@@ -338,7 +341,7 @@ __device__ int adjoint_point_ckpt(const Ctx<R>& c, const System<R>& sys, int q, 
         row_gemm<R, S>(dj, nl, dn, vop(sys, q, j), opN<R>(sZn, ld), EpiStore<R>{s1, ld, mk<R>(1, 0)});
         row_gemm<R, S>(dj, nl, dj, opC<R>(gj, ld), opN<R>(s1, ld), EpiAddStore<R>{sZ, ld, yj, ld});
       }
-      row_gemm<R, S>(dj, nl, nr, opN<R>(xc, ld), opN<R>(sl.W, ld), EpiStore<R>{kc, ld, mk<R>(1, 0)});
+      row_gemm<R, S>(dj, nl, nr, opN<R>(xc, ld), opN<R>(s2, ld), EpiStore<R>{kc, ld, mk<R>(1, 0)});
       if (j >= 1 && j <= L) {
         row_gemm<R, S>(dj, dj, nl, opN<R>(kc, ld), opC<R>(sZ, ld),
                        EpiAtomic{go.gHd + ((size_t)q * L + (j - 1)) * n * n, n, s2w, false});
