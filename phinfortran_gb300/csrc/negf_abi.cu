@@ -704,13 +704,23 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, kLayerCtasPerSm)
         const fcx* H = (j <= L) ? sys.fHd + ((size_t)q * L + (j - 1)) * sys.n * sys.n : sys.fHR + (size_t)q * nr * nr;
         const int ldh = (j <= L) ? sys.n : nr;
         const fcx* Sr = lo.fsr + p * B;
+        // H_j (+ Sigma_R) into Y first: the loads of a whole row are in flight
+        // together instead of one per epilogue column
+#pragma unroll
+        for (int c = 0; c < NW; ++c) {
+          fcx h = fz();
+          if (lane < dj && c < dj) {
+            h = H[lane + (size_t)c * ldh];
+            if (j == L + 1) h = pf::cadd(h, Sr[lane + c * NW]);
+          }
+          Y[lane + c * LDW] = h;
+        }
         rgemm(a, X, lane, [&](int r, int c, fcx u) {             // A_j from V^H T
           fcx v;
           if (r < dj && c < dj) {
             v = pf::mk<float>(-u.x, -u.y);
             if (r == c) v = pf::cadd(v, zf);
-            v = pf::csub(v, H[r + (size_t)c * ldh]);
-            if (j == L + 1) v = pf::csub(v, Sr[r + c * NW]);
+            v = pf::csub(v, Y[r + c * LDW]);
           } else {
             v = pf::mk<float>(r == c ? 1.f : 0.f, 0.f);
           }
@@ -750,8 +760,10 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, kLayerCtasPerSm)
           __syncwarp();
           row_smem_h(Y, lane, a);                                // row of V_{j-1}^H
           __syncwarp();
+#pragma unroll
+          for (int c = 0; c < NW; ++c) Y[lane + c * LDW] = yv[(size_t)j * B + lane + c * NW];   // r_j
           rgemm(a, X, lane, [&](int r, int c, fcx v) {           // u = r_j + V^H y_{j-1}
-            Y[r + c * LDW] = pf::cadd(v, yv[(size_t)j * B + r + c * NW]);
+            Y[r + c * LDW] = pf::cadd(v, Y[r + c * LDW]);
           });
           __syncwarp();
         }
@@ -774,13 +786,19 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, kLayerCtasPerSm)
         rgemm(a, X, lane, [&](int r, int c, fcx v) { Y[r + c * LDW] = v; });  // t = V_j d_{j+1}
         __syncwarp();
         row_block(lu + (size_t)j * B, lane, a);
+#pragma unroll
+        for (int c = 0; c < NW; ++c) X[lane + c * LDW] = yv[(size_t)j * B + lane + c * NW];   // y_j
         rgemm(a, Y, lane, [&](int r, int c, fcx v) {             // d_j = y_j + g_j t
-          v = pf::cadd(v, yv[(size_t)j * B + r + c * NW]);
-          X[r + c * LDW] = v;
-          dcx& x = xv[(size_t)j * B + r + c * NW];
-          x.x = x.x + pf::df64(v.x, 0.f);
-          x.y = x.y + pf::df64(v.y, 0.f);
+          X[r + c * LDW] = pf::cadd(v, X[r + c * LDW]);
         });
+        // X += d, all 32 loads of the row in flight together
+#pragma unroll
+        for (int c = 0; c < NW; ++c) {
+          dcx& x = xv[(size_t)j * B + lane + c * NW];
+          const fcx d = X[lane + c * LDW];
+          x.x = x.x + pf::df64(d.x, 0.f);
+          x.y = x.y + pf::df64(d.y, 0.f);
+        }
         __syncwarp();
       }
     }
