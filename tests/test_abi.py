@@ -43,3 +43,20 @@ def test_version_and_error_without_gpu(built_lib):
                               0.0, 0.0, 1.0, 1e-14, 10, 0, None, None, None, None)
     assert rc == -1
     assert b"positive" in lib.pf_last_error()
+
+
+def test_argument_validation_of_later_entries_without_gpu(built_lib):
+    """The full-Hamiltonian, tight-binding and Buttiker-probe entries reject
+    bad sizes on the host before touching a device."""
+    from phinfortran_gb300 import _abi
+    lib = _abi.load()
+    rc = lib.pf_gen_dyn(0, 1, 1, 1, 1, 3, 3, None, None, 0, None, None, None, None, 1, None, 1, None)
+    assert rc == -1 and b"positive" in lib.pf_fullh_last_error()
+    rc = lib.pf_gen_dyn(4, 1, 1, 3, 2, 9, 9, None, None, 0, None, None, None, None, 1, None, 1, None)
+    assert rc == -1 and b"multiple of nz" in lib.pf_fullh_last_error()
+    rc = lib.pf_buttiker_tdb(4, 4, 4, 1, 1, *([None] * 8), 1, None, None, None, *([None] * 6),
+                             0.0, 0.0, 10.0, 1e-14, 10, *([None] * 7), None)
+    assert rc == -1 and b"two device layers" in lib.pf_buttiker_last_error()
+    rc = lib.pf_buttiker_tdb(64, 4, 4, 3, 1, *([None] * 8), 1, None, None, None, *([None] * 6),
+                             0.0, 0.0, 10.0, 1e-14, 10, *([None] * 7), None)
+    assert rc == -3
