@@ -342,10 +342,13 @@ enum : int {
   PF_NOT_CONVERGED = 4,  // decimation hit its iteration cap
 };
 
-// In-place inverse of the n x n matrix M (ld odd, shared memory).
-// Returns PF_OK, PF_SINGULAR or PF_NAN (uniform across the CTA).
+// In-place inverse with explicit row exchanges (pivot rows swapped into
+// place, every thread filling the pivot row and column, four barriers a
+// step, the column interchanges undone one by one).  With 16 warps a CTA
+// the parallel fill beats warp 0 preparing the pivot row (measured on the
+// 512-thread gradient and fused mixed kernels), so inverse() uses it there.
 template <typename R>
-__device__ int inverse(cx<R>* M, int ld, int n, InvWork<R> w) {
+__device__ int inverse_swap(cx<R>* M, int ld, int n, InvWork<R> w) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5;
   int status = PF_OK;
@@ -424,6 +427,106 @@ __device__ int inverse(cx<R>* M, int ld, int n, InvWork<R> w) {
         M[i + p * ld] = t;
       }
     }
+    __syncthreads();
+  }
+  return status;
+}
+
+// In-place inverse of the n x n matrix M (ld odd, shared memory, n <= 1024).
+// Gauss-Jordan with implicit partial pivoting: the pivot of step k is the
+// first maximum of |re|+|im| in column k among the rows not yet used
+// (LAPACK izamax's measure); rows are never exchanged, warp 0 prepares the
+// scaled pivot row and the pivot column, and every thread then updates its
+// elements -- two barriers a step.  The row/column permutation is undone at
+// the end by one gather: inv(k, P(j)) = M(P(k), j).
+// Returns PF_OK, PF_SINGULAR or PF_NAN (uniform across the CTA).
+template <typename R>
+__device__ int inverse(cx<R>* M, int ld, int n, InvWork<R> w) {
+  if (blockDim.x > 256) return inverse_swap(M, ld, n, w);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  int status = PF_OK;
+  unsigned used = 0u;  // warp 0, lane l: bit m set when row l + 32 m is pivoted
+  for (int k = 0; k < n; ++k) {
+    if (warp == 0) {
+      double best = -1.0;
+      int bi = n;
+      for (int i = lane; i < n; i += 32) {
+        if ((used >> (i >> 5)) & 1u) continue;
+        const double v = cabs1(M[i + k * ld]);
+        const double vv = (v != v) ? 3.0e300 : v;  // NaN wins so it gets reported
+        if (vv > best) {
+          best = vv;
+          bi = i;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      const int p = bi;
+      if ((p & 31) == lane) used |= 1u << (p >> 5);
+      const cx<R> ip = crecip(M[p + k * ld]);
+      for (int j = lane; j < n; j += 32) {
+        w.rowk[j] = (j == k) ? ip : cmul(M[p + j * ld], ip);
+        w.colk[j] = M[j + k * ld];
+      }
+      if (lane == 0) {
+        w.perm[k] = p;
+        w.flag[0] = p;
+      }
+    }
+    __syncthreads();
+    const int p = w.flag[0];
+    const cx<R> piv = w.colk[p];
+    if (piv.x == R(0) && piv.y == R(0)) status |= PF_SINGULAR;
+    if (!(isfinite(piv.x) && isfinite(piv.y))) status |= PF_NAN;
+    const cx<R> ip = w.rowk[k];
+    for (int i = tid; i < n * n; i += nt) {
+      const int r = i % n, c = i / n;
+      if (r == p) {
+        M[r + c * ld] = w.rowk[c];
+      } else if (c == k) {
+        const cx<R> f = w.colk[r];
+        M[r + c * ld] = mk<R>(-(f.x * ip.x - f.y * ip.y), -(f.x * ip.y + f.y * ip.x));
+      } else {
+        const cx<R> f = w.colk[r];
+        const cx<R> rk = w.rowk[c];
+        cx<R> v = M[r + c * ld];
+        v.x = fma(-f.x, rk.x, fma(f.y, rk.y, v.x));
+        v.y = fma(-f.x, rk.y, fma(-f.y, rk.x, v.y));
+        M[r + c * ld] = v;
+      }
+    }
+    __syncthreads();
+  }
+  // inv(k, P(j)) = M(P(k), j), as a row gather within each column and then a
+  // column scatter within each row; each pass goes through registers in
+  // chunks of whole columns (rows) of at most kMaxPer elements a thread,
+  // one chunk for n <= 64 with 128 or more threads.
+  constexpr int kMaxPer = 32;
+  cx<R> tmp[kMaxPer];
+  const int per = (kMaxPer * nt) / n > 0 ? (kMaxPer * nt) / n : 1;
+  for (int j0 = 0; j0 < n; j0 += per) {
+    const int nc = (j0 + per < n ? j0 + per : n) - j0;
+    int t = 0;
+    for (int i = tid; i < n * nc; i += nt, ++t) tmp[t] = M[w.perm[i % n] + (j0 + i / n) * ld];
+    __syncthreads();
+    t = 0;
+    for (int i = tid; i < n * nc; i += nt, ++t) M[i % n + (j0 + i / n) * ld] = tmp[t];
+    __syncthreads();
+  }
+  for (int k0 = 0; k0 < n; k0 += per) {
+    const int nrw = (k0 + per < n ? k0 + per : n) - k0;
+    int t = 0;
+    for (int i = tid; i < nrw * n; i += nt, ++t) tmp[t] = M[k0 + i % nrw + (i / nrw) * ld];
+    __syncthreads();
+    t = 0;
+    for (int i = tid; i < nrw * n; i += nt, ++t) M[k0 + i % nrw + w.perm[i / nrw] * ld] = tmp[t];
     __syncthreads();
   }
   return status;
