@@ -280,7 +280,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--path", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--refine", type=int, default=1, help="refinement sweeps of the mixed path")
+    ap.add_argument("--refine", type=int, default=2,
+                    help="maximum refinement sweeps of the mixed path (sweeps after the first are adaptive)")
     ap.add_argument("--ref-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -439,8 +440,10 @@ def main():
         launches_per_step = 2                         # lead-mirror check + transport_kernel
     else:
         # 8 block conversions + 7 ELL builds + lead-mirror check + leads_kernel + layer_kernel (factor)
-        # + per refinement (residual_kernel + layer_kernel) + point-energy kernel + layer_kernel (Caroli)
-        launches_per_step = 8 + 7 + 1 + 1 + 1 + 2 * args.refine + (1 if args.refine else 0) + 1
+        # + the first refinement sweep (residual_kernel + layer_kernel) + each later, adaptive sweep
+        # (refine_select_kernel + residual_kernel + layer_kernel) + point-energy kernel + layer_kernel (Caroli)
+        sweeps = (2 + 3 * (args.refine - 1) + 1) if args.refine else 0
+        launches_per_step = 8 + 7 + 1 + 1 + 1 + sweeps + 1
     line = dict(metric=METRIC, value=value, unit="solves/s", n_gpus=ws, steps=args.steps, warmup=args.warmup,
                 ms_per_step=t_step * 1e3, higher_is_better=True, scaling="weak", vs_baseline=None,
                 dtype="complex128 (fp64)" if args.path == "fp64" else "complex: fp32 + double-float (no fp64 ops)",

@@ -125,7 +125,10 @@ int pf_transport_tdb(int n, int nl, int nr, int L, int nq,
  *   - the device blocks are factorised in FP32 (the left-connected
  *     recursion of negf/lesser.f90:547-654 as a block LU of the extended
  *     lead+device matrix), and the last block column G_{:,N+1} is refined
- *     `refine_iters` times against a double-float residual;
+ *     against a double-float residual: one sweep for every point, then up
+ *     to refine_iters - 1 more for each point whose last correction of the
+ *     block X_0 = G_{0,N+1} was above 1e-5 relative to X_0 (refine_iters
+ *     in [0, 16]; 0 keeps the FP32 solution);
  *   - the Caroli trace (negf/lesser.f90:787-792) is taken in double-float.
  * The per-point matrix work uses no FP64 arithmetic.  work must hold
  * pf_transport_tdb_mixed_workspace_size(...) bytes.

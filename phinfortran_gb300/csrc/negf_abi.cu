@@ -396,7 +396,10 @@ __global__ void __launch_bounds__(kMixedThreads) mixed_kernel(pf::MSys sys, pf::
     st |= pf::mixed_factor_solve<S>(c, sys, q, zf);
     const dcx zL = pf::mk<pf::df64>(pf::df64(E), pf::df64(eps));
     const dcx zD = pf::mk<pf::df64>(pf::df64(E), pf::df64(P.dev_factor * eps));
-    for (int k = 0; k < nref; ++k) pf::mixed_refine<S>(c, sys, q, zL, zD);
+    // the first sweep always; later ones while the last correction of X_0
+    // was above PF_REFINE_TOL
+    for (int k = 0; k < nref; ++k)
+      if (!pf::mixed_refine<S>(c, sys, q, zL, zD)) break;
     const double tl = pf::mixed_caroli<S>(c, sys);
     if (threadIdx.x == 0) {
       const bool zero = pts.zero_flag && pts.zero_flag[p];
@@ -564,8 +567,18 @@ __global__ void point_z_kernel(pf::Points pts, pf::Params P, dcx* z2) {
   z2[2 * p + 1] = pf::mk<pf::df64>(pf::df64(E), pf::df64(P.dev_factor * eps));
 }
 
+// Points whose last refinement sweep left a correction above PF_REFINE_TOL
+// (order is irrelevant: every point is solved independently).
+__global__ void refine_select_kernel(int npts, const float* corr, int* list, int* count) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npts || !(corr[p] > pf::PF_REFINE_TOL)) return;
+  list[atomicAdd(count, 1)] = p;
+}
+
+template <bool kList>
 __global__ void __launch_bounds__(kResThreads)
-    residual_kernel(pf::MSys s, pf::Points pts, const dcx* z2, pf::wp::LeadOut lo, pf::wp::Slabs sl) {
+    residual_kernel(pf::MSys s, pf::Points pts, const dcx* z2, pf::wp::LeadOut lo, pf::wp::Slabs sl,
+                    const int* list, const int* count) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   dcx* win = reinterpret_cast<dcx*>(smem_raw);
   constexpr int NW = pf::wp::NW;
@@ -574,8 +587,10 @@ __global__ void __launch_bounds__(kResThreads)
   const int r = threadIdx.x % NW, c0 = threadIdx.x / NW;
   const int runs = (nb + kResLayers - 1) / kResLayers;
   const bool sparse = s.ell_overflow != nullptr && *s.ell_overflow == 0;
-  for (int task = blockIdx.x; task < pts.npts * runs; task += gridDim.x) {
-    const int p = task / runs;
+  // kList: the points of an adaptive refinement sweep are list[0 .. *count)
+  const int np = kList ? *count : pts.npts;
+  for (int task = blockIdx.x; task < np * runs; task += gridDim.x) {
+    const int p = kList ? list[task / runs] : task / runs;
     const int j0 = (task % runs) * kResLayers;
     const int j1 = j0 + kResLayers < nb ? j0 + kResLayers : nb;
     const int q = pts.qidx ? pts.qidx[p] : 0;
@@ -655,9 +670,94 @@ __global__ void __launch_bounds__(kResThreads)
   }
 }
 
+constexpr int kSplitCols = pf::wp::NW / kWarpsPerCta;
+
+// One refinement sweep of a point over the NC solution columns
+// [cb, cb + NC): NC = 32 when a warp owns the point, kSplitCols when the
+// warps of a CTA share it (the columns are independent right-hand sides).
+//   forward:  y_j = g_j (r_j + V_{j-1}^H y_{j-1})   (r_j in yv[j] on entry)
+//   backward: d_{L+1} = y_{L+1}; d_j = y_j + g_j V_j d_{j+1}; X += d
+// md, mx: the largest |d_0| and |X_0| over rows < nl and these columns
+// (warp-reduced).
+template <int NC>
+__device__ __forceinline__ void refine_sweep(const pf::MSys& sys, int q, int lane, int cb, fcx* X, fcx* Y,
+                                             const fcx* lu, fcx* yv, dcx* xv, float& md, float& mx) {
+  using namespace pf::wp;
+  const int L = sys.L;
+  const size_t B = (size_t)NW * NW;
+  fcx a[NW];
+#pragma unroll
+  for (int i = 0; i < NC; ++i) Y[lane + (cb + i) * LDW] = yv[lane + (cb + i) * NW];
+  __syncwarp();
+  for (int j = 0; j <= L + 1; ++j) {
+    if (j >= 1) {
+      stage_rows(Y, vview(sys, q, j - 1), lane);
+      __syncwarp();
+      row_smem_h(Y, lane, a);                                    // row of V_{j-1}^H
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < NC; ++i) Y[lane + (cb + i) * LDW] = yv[(size_t)j * B + lane + (cb + i) * NW];   // r_j
+      rgemm_cols<NC>(a, X, lane, cb, [&](int r, int c, fcx v) {  // u = r_j + V^H y_{j-1}
+        Y[r + c * LDW] = pf::cadd(v, Y[r + c * LDW]);
+      });
+      __syncwarp();
+    }
+    row_block(lu + (size_t)j * B, lane, a);
+    rgemm_cols<NC>(a, Y, lane, cb, [&](int r, int c, fcx v) {    // y_j = g_j u
+      X[r + c * LDW] = v;
+      yv[(size_t)j * B + r + c * NW] = v;
+    });
+    __syncwarp();
+  }
+#pragma unroll
+  for (int i = 0; i < NC; ++i) {
+    dcx& x = xv[(size_t)(L + 1) * B + lane + (cb + i) * NW];
+    const fcx d = X[lane + (cb + i) * LDW];
+    x.x = x.x + pf::df64(d.x, 0.f);
+    x.y = x.y + pf::df64(d.y, 0.f);
+  }
+  for (int j = L; j >= 0; --j) {
+    row_view(vview(sys, q, j), lane, a);
+    rgemm_cols<NC>(a, X, lane, cb, [&](int r, int c, fcx v) { Y[r + c * LDW] = v; });  // t = V_j d_{j+1}
+    __syncwarp();
+    row_block(lu + (size_t)j * B, lane, a);
+#pragma unroll
+    for (int i = 0; i < NC; ++i) X[lane + (cb + i) * LDW] = yv[(size_t)j * B + lane + (cb + i) * NW];   // y_j
+    rgemm_cols<NC>(a, Y, lane, cb, [&](int r, int c, fcx v) {    // d_j = y_j + g_j t
+      X[r + c * LDW] = pf::cadd(v, X[r + c * LDW]);
+    });
+    // X += d, all loads of the row in flight together
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+      dcx& x = xv[(size_t)j * B + lane + (cb + i) * NW];
+      const fcx d = X[lane + (cb + i) * LDW];
+      x.x = x.x + pf::df64(d.x, 0.f);
+      x.y = x.y + pf::df64(d.y, 0.f);
+    }
+    __syncwarp();
+  }
+  md = 0.f;
+  mx = 0.f;
+  if (lane < sys.nl) {
+    for (int i = 0; i < NC; ++i) {
+      const int c = cb + i;
+      if (c >= sys.nr) break;
+      const fcx d = X[lane + c * LDW];
+      const dcx x = xv[lane + c * NW];
+      md = fmaxf(md, fabsf(d.x) + fabsf(d.y));
+      mx = fmaxf(mx, fabsf(x.x.hi) + fabsf(x.y.hi));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, o));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+}
+
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kLayerCtasPerSm)
     layer_kernel(pf::MSys sys, pf::Points pts, pf::Params P, int phase, pf::Outputs out, pf::wp::LeadOut lo,
-                 pf::wp::Slabs sl, int* lead_status, int* queue) {
+                 pf::wp::Slabs sl, int* lead_status, int* queue, const int* list, const int* count) {
   using namespace pf::wp;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -666,17 +766,32 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, kLayerCtasPerSm)
   fcx* Y = X + LDW * NW;
   const int L = sys.L, nr = sys.nr;
   const size_t B = (size_t)NW * NW;
+  // list/count: the points of an adaptive refinement sweep (all points when null)
+  const int np = list ? *count : pts.npts;
+  // phase 3: a refinement sweep in which the CTA's warps share one point,
+  // each taking kSplitCols of the solution's columns
+  const bool split = (phase == 3);
+  __shared__ int s_pi;
+  __shared__ float2 s_red[kWarpsPerCta];
   for (;;) {
-    int p = 0;
-    if (lane == 0) p = atomicAdd(queue, 1);
-    p = __shfl_sync(0xffffffffu, p, 0);
-    if (p >= pts.npts) break;
+    int pi = 0;
+    if (split) {
+      __syncthreads();  // s_pi and s_red of the previous point are consumed
+      if (threadIdx.x == 0) s_pi = atomicAdd(queue, 1);
+      __syncthreads();
+      pi = s_pi;
+    } else {
+      if (lane == 0) pi = atomicAdd(queue, 1);
+      pi = __shfl_sync(0xffffffffu, pi, 0);
+    }
+    if (pi >= np) break;
+    const int p = list ? list[pi] : pi;
     const int q = pts.qidx ? pts.qidx[p] : 0;
     const double E = pts.E[p];
     const double eps = E * P.eta + P.eta0;
     const fcx zf = pf::mk<float>((float)E, (float)(P.dev_factor * eps));
     int st = lead_status[p];
-    const bool do_factor = (phase == 0), do_refine = (phase == 1), do_caroli = (phase == 2);
+    const bool do_factor = (phase == 0), do_refine = (phase == 1 || split), do_caroli = (phase == 2);
     fcx* lu = sl.lu + (size_t)p * (L + 2) * B;
     fcx* yv = sl.yv + (size_t)p * (L + 2) * B;
     dcx* xv = sl.xv + (size_t)p * (L + 2) * B;
@@ -751,56 +866,22 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, kLayerCtasPerSm)
     }  // do_factor
     // ---- one refinement sweep (the residual r_j was written into yv[j] by residual_kernel)
     if (do_refine) {
-      // forward: y_j = g_j (r_j + V_{j-1}^H y_{j-1}); y_{j-1} is kept in X
-      for (int c = 0; c < NW; ++c) Y[lane + c * LDW] = yv[lane + c * NW];
-      __syncwarp();
-      for (int j = 0; j <= L + 1; ++j) {
-        if (j >= 1) {
-          stage_rows(Y, vview(sys, q, j - 1), lane);
-          __syncwarp();
-          row_smem_h(Y, lane, a);                                // row of V_{j-1}^H
-          __syncwarp();
-#pragma unroll
-          for (int c = 0; c < NW; ++c) Y[lane + c * LDW] = yv[(size_t)j * B + lane + c * NW];   // r_j
-          rgemm(a, X, lane, [&](int r, int c, fcx v) {           // u = r_j + V^H y_{j-1}
-            Y[r + c * LDW] = pf::cadd(v, Y[r + c * LDW]);
-          });
-          __syncwarp();
+      float md, mx;
+      if (split) {
+        refine_sweep<kSplitCols>(sys, q, lane, w * kSplitCols, X, Y, lu, yv, xv, md, mx);
+        if (lane == 0) s_red[w] = make_float2(md, mx);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          for (int i = 1; i < kWarpsPerCta; ++i) {
+            md = fmaxf(md, s_red[i].x);
+            mx = fmaxf(mx, s_red[i].y);
+          }
         }
-        row_block(lu + (size_t)j * B, lane, a);
-        rgemm(a, Y, lane, [&](int r, int c, fcx v) {             // y_j = g_j u
-          X[r + c * LDW] = v;
-          yv[(size_t)j * B + r + c * NW] = v;
-        });
-        __syncwarp();
+      } else {
+        refine_sweep<NW>(sys, q, lane, 0, X, Y, lu, yv, xv, md, mx);
       }
-      // backward: d_{L+1} = y_{L+1}; d_j = y_j + g_j V_j d_{j+1}; X += d (d_{j+1} kept in X)
-      for (int c = 0; c < NW; ++c) {
-        dcx& x = xv[(size_t)(L + 1) * B + lane + c * NW];
-        const fcx d = X[lane + c * LDW];
-        x.x = x.x + pf::df64(d.x, 0.f);
-        x.y = x.y + pf::df64(d.y, 0.f);
-      }
-      for (int j = L; j >= 0; --j) {
-        row_view(vview(sys, q, j), lane, a);
-        rgemm(a, X, lane, [&](int r, int c, fcx v) { Y[r + c * LDW] = v; });  // t = V_j d_{j+1}
-        __syncwarp();
-        row_block(lu + (size_t)j * B, lane, a);
-#pragma unroll
-        for (int c = 0; c < NW; ++c) X[lane + c * LDW] = yv[(size_t)j * B + lane + c * NW];   // y_j
-        rgemm(a, Y, lane, [&](int r, int c, fcx v) {             // d_j = y_j + g_j t
-          X[r + c * LDW] = pf::cadd(v, X[r + c * LDW]);
-        });
-        // X += d, all 32 loads of the row in flight together
-#pragma unroll
-        for (int c = 0; c < NW; ++c) {
-          dcx& x = xv[(size_t)j * B + lane + c * NW];
-          const fcx d = X[lane + c * LDW];
-          x.x = x.x + pf::df64(d.x, 0.f);
-          x.y = x.y + pf::df64(d.y, 0.f);
-        }
-        __syncwarp();
-      }
+      const bool writer = split ? threadIdx.x == 0 : lane == 0;
+      if (writer) sl.corr[p] = mx > 0.f ? md / mx : (md > 0.f ? INFINITY : 0.f);
     }
     if (do_factor) {
       if (lane == 0) lead_status[p] = st;
@@ -857,8 +938,9 @@ struct MixedPlan {
   bool warp_engine;     // cross-sections <= 32: leads kernel + warp-per-point layer kernel
   int grid_a, grid_b;   // CTA counts of the (leads / fused) kernel and the layer kernel
   int grid_r;           // resident CTAs of the residual kernel
+  int grid_s;           // CTAs of the split refinement sweeps (a CTA per listed point)
   size_t per_cta_a;     // per-CTA scratch of kernel A
-  size_t off_blocks, off_ell, off_scratch, off_lead, off_lstat, off_z, off_slabs, total;
+  size_t off_blocks, off_ell, off_scratch, off_lead, off_lstat, off_z, off_refine, off_slabs, total;
   size_t smem_b;
 };
 
@@ -901,11 +983,14 @@ bool make_plan(int n, int nl, int nr, int L, int nq, int npts, MixedPlan& P) {
     int gb = d.sms * per_sm;
     const int need_ctas = (warps + kWarpsPerCta - 1) / kWarpsPerCta;
     P.grid_b = gb < need_ctas ? gb : need_ctas;
-    if (cudaFuncSetAttribute(residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kResSmem) !=
-        cudaSuccess)
+    P.grid_s = gb < np ? gb : np;
+    if (cudaFuncSetAttribute(residual_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kResSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(residual_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kResSmem) !=
+            cudaSuccess)
       return false;
     int per_sm_r = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_r, residual_kernel, kResThreads, kResSmem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_r, residual_kernel<false>, kResThreads, kResSmem) !=
             cudaSuccess ||
         per_sm_r < 1)
       return false;
@@ -915,6 +1000,7 @@ bool make_plan(int n, int nl, int nr, int L, int nq, int npts, MixedPlan& P) {
     P.per_cta_a = lay.per_cta;
     P.grid_b = 0;
     P.grid_r = 0;
+    P.grid_s = 0;
     P.smem_b = 0;
   }
   if (P.grid_a <= 0) return false;
@@ -931,6 +1017,8 @@ bool make_plan(int n, int nl, int nr, int L, int nq, int npts, MixedPlan& P) {
   if (P.warp_engine) o += al256((size_t)np * sizeof(int));
   P.off_z = o;
   if (P.warp_engine) o += al256((size_t)np * 2 * 16);
+  P.off_refine = o;  // per-point relative corrections and the compacted point list
+  if (P.warp_engine) o += al256((size_t)np * 2 * sizeof(int));
   P.off_slabs = o;
   if (P.warp_engine) o += al256((size_t)np * (L + 2) * Bn * (8 + 8 + 16));
   P.total = o;
@@ -1290,27 +1378,48 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq, const doubl
     sl.lu = reinterpret_cast<fcx*>(w + plan.off_slabs);
     sl.yv = sl.lu + np * (L + 2) * Bn;
     sl.xv = reinterpret_cast<dcx*>(sl.yv + np * (L + 2) * Bn);
+    sl.corr = reinterpret_cast<float*>(w + plan.off_refine);
+    int* rlist = reinterpret_cast<int*>(sl.corr + np);
+    int* rcount = queue + 2;
     leads_kernel<1><<<plan.grid_a, kThreads, lay.smem_leads, st>>>(sys, pts, P, out, lay, plan.per_cta_a, scratch, lo,
                                                               lstat, queue);
     PF_CUDA(cudaGetLastError());
     // factorisation + back substitution, then each refinement sweep as a
     // parallel residual kernel followed by the warp-per-point correction,
     // then the Caroli trace
-    layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 0, out, lo, sl, lstat, queue_b);
+    layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 0, out, lo, sl, lstat, queue_b,
+                                                                       nullptr, nullptr);
     PF_CUDA(cudaGetLastError());
     const long rtasks = (long)npts * ((L + 2 + kResLayers - 1) / kResLayers);
     const int rblocks = (int)(rtasks < (long)plan.grid_r ? rtasks : (long)plan.grid_r);
     dcx* z2 = reinterpret_cast<dcx*>(w + plan.off_z);
     if (refine_iters > 0) point_z_kernel<<<(npts + 127) / 128, 128, 0, st>>>(pts, P, z2);
     for (int it = 0; it < refine_iters; ++it) {
-      residual_kernel<<<rblocks, kResThreads, kResSmem, st>>>(sys, pts, z2, lo, sl);
+      // the first sweep covers every point, later ones the points whose
+      // previous correction was above PF_REFINE_TOL (grids sized for all
+      // points; the kernels read the count on the device)
+      const int* lst = nullptr;
+      const int* cnt = nullptr;
+      if (it > 0) {
+        PF_CUDA(cudaMemsetAsync(rcount, 0, sizeof(int), st));
+        refine_select_kernel<<<(npts + 255) / 256, 256, 0, st>>>(npts, sl.corr, rlist, rcount);
+        lst = rlist;
+        cnt = rcount;
+      }
+      if (it > 0)
+        residual_kernel<true><<<rblocks, kResThreads, kResSmem, st>>>(sys, pts, z2, lo, sl, lst, cnt);
+      else
+        residual_kernel<false><<<rblocks, kResThreads, kResSmem, st>>>(sys, pts, z2, lo, sl, nullptr, nullptr);
       PF_CUDA(cudaMemsetAsync(queue_b, 0, sizeof(int), st));
-      layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 1, out, lo, sl, lstat,
-                                                                         queue_b);
+      // later sweeps cover few points: a CTA per point, its warps splitting
+      // the columns, shortens each point's sequential sweep
+      layer_kernel<<<it > 0 ? plan.grid_s : plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(
+          sys, pts, P, it > 0 ? 3 : 1, out, lo, sl, lstat, queue_b, lst, cnt);
       PF_CUDA(cudaGetLastError());
     }
     PF_CUDA(cudaMemsetAsync(queue_b, 0, sizeof(int), st));
-    layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 2, out, lo, sl, lstat, queue_b);
+    layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 2, out, lo, sl, lstat, queue_b,
+                                                                       nullptr, nullptr);
   } else if (S == 1) {
     mixed_kernel<1><<<plan.grid_a, kMixedThreads, lay.smem, st>>>(sys, pts, P, refine_iters, out, lay, scratch, queue);
   } else {

@@ -41,6 +41,7 @@ struct Slabs {
   fcx* lu;   // [pts][L+2][32*32] FP32 factors
   fcx* yv;   // [pts][L+2][32*32] FP32 forward vectors
   dcx* xv;   // [pts][L+2][32*32] df64 solution blocks
+  float* corr; // [pts] size of the last sweep's correction of X_0 relative to X_0
 };
 
 __device__ __forceinline__ fcx fz() { return mk<float>(0.f, 0.f); }
@@ -81,6 +82,29 @@ __device__ __forceinline__ void rgemm(const fcx (&a)[NW], const fcx* B, int lane
   constexpr int U = 4;  // columns per step: 8 independent FMA chains per lane
 #pragma unroll 1
   for (int c0 = 0; c0 < NW; c0 += U) {
+    fcx acc0[U], acc1[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc0[u] = acc1[u] = fz();
+#pragma unroll
+    for (int k = 0; k < NW; k += 2) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const float4 b = *reinterpret_cast<const float4*>(B + k + (c0 + u) * LDW);
+        acc0[u] = ffma(a[k], mk<float>(b.x, b.y), acc0[u]);
+        acc1[u] = ffma(a[k + 1], mk<float>(b.z, b.w), acc1[u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) epi(lane, c0 + u, cadd(acc0[u], acc1[u]));
+  }
+}
+
+// rgemm over the NC columns [cb, cb + NC) of B only (NC a multiple of 4).
+template <int NC, class Epi>
+__device__ __forceinline__ void rgemm_cols(const fcx (&a)[NW], const fcx* B, int lane, int cb, Epi epi) {
+  constexpr int U = 4;
+#pragma unroll 1
+  for (int c0 = cb; c0 < cb + NC; c0 += U) {
     fcx acc0[U], acc1[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) acc0[u] = acc1[u] = fz();

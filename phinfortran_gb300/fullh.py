@@ -311,7 +311,7 @@ class FullH:
         return dev, (n, nl, nr, L, nq)
 
     def transport(self, E, kfrac, qidx=None, *, eta, eta0, convergence, dev_factor=10.0, max_iter=1000,
-                  precision="fp64", refine_iters=1):
+                  precision="fp64", refine_iters=2):
         """T_L of every point (E[p] at k = kfrac[qidx[p]]): D(q) built and
         sliced on the GPU, then the tdb transport engine on device blocks."""
         from .transport import DeviceTransport

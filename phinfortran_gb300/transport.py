@@ -123,15 +123,16 @@ def _transport_tiled(E, nq, dims, arrs, *, eta, eta0, convergence, dev_factor, q
 
 def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=None,
                   zero_flag=None, max_iter=1000, want_transr=True, check=True,
-                  precision="fp64", refine_iters=1):
+                  precision="fp64", refine_iters=2):
     """Transmission for a batch of points through the host-pointer C entry.
 
     E: (npts,) energies (omega^2 for phonons).  blocks: TdbBlocks or dict.
     qidx: (npts,) q index into the stacked blocks (None: all 0).
     zero_flag: (npts,) nonzero -> T forced to 0 (the reference's ie == 1).
     precision: "fp64" (pf_transport_tdb) or "mixed" (pf_transport_tdb_mixed:
-    double-float leads, FP32 factorisation, `refine_iters` double-float
-    refinement sweeps; T_L only).
+    double-float leads, FP32 factorisation, double-float refinement: one
+    sweep for every point and up to `refine_iters` - 1 more for the points
+    whose last correction of G_{0,N+1} was above 3e-5 relative; T_L only).
     Returns dict(transl, transr, status, iters).
     """
     if precision not in ("fp64", "mixed"):
@@ -180,7 +181,7 @@ class DeviceTransport:
     """
 
     def __init__(self, blocks, npts_max, *, eta, eta0, convergence, dev_factor=10.0,
-                 max_iter=1000, want_transr=False, device="cuda", precision="fp64", refine_iters=1):
+                 max_iter=1000, want_transr=False, device="cuda", precision="fp64", refine_iters=2):
         import torch
         if isinstance(blocks, dict):
             blocks = TdbBlocks.from_dict(blocks)
@@ -200,7 +201,7 @@ class DeviceTransport:
         return obj
 
     def _setup(self, dev, dims, npts_max, *, eta, eta0, convergence, dev_factor=10.0, max_iter=1000,
-               want_transr=False, device="cuda", precision="fp64", refine_iters=1):
+               want_transr=False, device="cuda", precision="fp64", refine_iters=2):
         import torch
         self.torch = torch
         lib = _abi.load()
