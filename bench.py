@@ -428,8 +428,9 @@ def main():
     if os.path.exists(prof):
         with open(prof) as f:
             pj = json.load(f)
-        roof["traffic"] = pj.get("dram_bytes_per_launch_scaled")
-        roof["traffic_source"] = pj.get("source")
+        if args.path == "fp64" or pj.get("refine_iters") == args.refine:
+            roof["traffic"] = pj.get("dram_bytes_per_launch_scaled")
+            roof["traffic_source"] = pj.get("source")
 
     cpu = None
     if not args.no_cpu_baseline:
