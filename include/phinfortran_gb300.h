@@ -328,7 +328,48 @@ int pf_transport_tdb_modes_dev(int n, int nl, int nr, int L, int nq,
                                double* mode_sums, int* status, int* nprop,
                                void* work, size_t work_bytes, void* stream);
 
-/* Message for the last error of the mode-resolved entry point. */
+/*
+ * pf_transport_tdb_modes_dev plus the per-mode data of the reference's
+ * per-k mode files (write_specular / write_md, negf/write_data.f90:3-176,
+ * called from negf/velocity_mat.f90:3108-3128), with mm = max(nl, nr) and
+ * the four problems in the order adv-L, ret-L, ret-R, adv-R:
+ *   mode_kz  [npts][4][mm]  k_z of every Bloch mode (k_z_L_ret etc.,
+ *                           velocity_mat.f90:2360), 100 when the mode is
+ *                           not propagating; modes in the order of this
+ *                           library's eigen-solver
+ *   mode_bz  [npts][4][mm]  unfolding label (bz_idx_*, 1-based; 0 when not
+ *                           propagating)
+ *   col_sums [npts][4][mm][nshift]  for the matrices tlr, trl, rrr, rll
+ *                           (rows: the outgoing modes, columns: the
+ *                           incoming ones) the sum of |M_rc|^2 over the
+ *                           rows r of each label, per labelled column c
+ * The in-plane k of a label is move_in_ws2((k_sc + shift) . recivec) and
+ * depends on the label only, so the specular test of write_specular
+ * (|k_f - k_b|^2 < 1e-5 in plane) is decided per label on the host.  All
+ * three pointers are given or all are null.
+ */
+int pf_transport_tdb_modes_permode_dev(int n, int nl, int nr, int L, int nq,
+                                       const double* HL, const double* HLv,
+                                       const double* HR, const double* HRv,
+                                       const double* Hd, const double* Hdv,
+                                       const double* Hld, const double* Hrd,
+                                       int npts, const double* E,
+                                       const int* qidx, const int* zero_flag,
+                                       double eta, double eta0,
+                                       double dev_factor, double convergence,
+                                       int max_iter, double lambda_eta,
+                                       double a_z_l, double a_z_r, int nshift,
+                                       int stride_l, int nrep_l,
+                                       const double* phase_l, int stride_r,
+                                       int nrep_r, const double* phase_r,
+                                       double* transl, double* transr,
+                                       double* mode_sums, int* status,
+                                       int* nprop, double* mode_kz,
+                                       int* mode_bz, double* col_sums,
+                                       void* work, size_t work_bytes,
+                                       void* stream);
+
+/* Message for the last error of the mode-resolved entry points. */
 const char* pf_modes_last_error(void);
 
 /*

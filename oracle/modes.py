@@ -219,3 +219,69 @@ def vel_mat_tdb(E, first, blocks, surf, rgf, geom, eta, eta0, lambda_eta):
     out["refll_s"], out["refll_ns"] = split_sums(rll, rL["bz"], aL["bz"])
     out.update(trl=trl, tlr=tlr, rrr=rrr, rll=rll, modes=dict(adv_l=aL, ret_l=rL, ret_r=rR, adv_r=aR))
     return out
+
+
+def k_xyz(mode, ksc, recivec, reci_uc, nb):
+    """velocity_mat.f90:2353-2360: the unfolded in-plane k of every
+    propagating mode (its label's shift) with z = k_z; 100 elsewhere."""
+    shifts = [(i, j) for i in range(nb[0]) for j in range(nb[1])]
+    k = np.full((mode["kz"].size, 3), 100.0)
+    for i in mode["prop"]:
+        sx, sy = shifts[mode["bz"][i] - 1]
+        k[i] = move_in_ws2((np.array([sx, sy, 0.0]) + ksc) @ recivec, reci_uc)
+        k[i, 2] = mode["kz"][i]
+    return k
+
+
+def _spec_sums(r, kf, kb, i):
+    """The r_s / r_t loop of negf/write_data.f90:39-57 for incoming mode i."""
+    rt = rs = 0.0
+    for j in range(kf.shape[0]):
+        if kf[j, 2] < 99.9:
+            a = abs(r[j, i]) ** 2
+            rt += a
+            d = kf[j] - kb[i]
+            d[2] = 0.0
+            if d @ d < 1.0e-5:
+                rs += a
+    rt = 1.0e-60 if 0.0 < rt < 1.0e-60 else rt
+    rs = 1.0e-60 if 0.0 < rs < 1.0e-60 else rs
+    return rs, rt
+
+
+def write_specular_rows(w, r, kf, kb):
+    """negf/write_data.f90:3-76 (k_pc and v_pc columns as zero)."""
+    rows, c = [], 0
+    for i in range(kb.shape[0]):
+        if kb[i, 2] < 99.9:
+            c += 1
+            rs, rt = _spec_sums(r, kf, kb, i)
+            rows.append((c, w, *kb[i], *(0.0,) * 6, rs, rt, rs / rt if rt != 0.0 else 0.0))
+    return rows
+
+
+def write_md_rows(w, t, r, kft, kf, kb):
+    """negf/write_data.f90:78-176 (k_pc and v_pc columns as zero)."""
+    rows, c = [], 0
+    for i in range(kb.shape[0]):
+        if kb[i, 2] < 99.9:
+            c += 1
+            rs, rt = _spec_sums(r, kf, kb, i)
+            ts, tt = _spec_sums(t, kft, kb, i)
+            rows.append((c, w, *kb[i], *(0.0,) * 6, rs, rt, ts, tt))
+    return rows
+
+
+def mode_file_rows(E, o, geom):
+    """Rows of the six per-k files for one point of vel_mat_tdb
+    (velocity_mat.f90:3108-3128)."""
+    g = geom
+    md = o["modes"]
+    kl = lambda m: k_xyz(m, g["ksc"], g["recivec"], g["reci_uc_l"], g["nb"])
+    kr = lambda m: k_xyz(m, g["ksc"], g["recivec"], g["reci_uc_r"], g["nb"])
+    kLr, kLa, kRr, kRa = kl(md["ret_l"]), kl(md["adv_l"]), kr(md["ret_r"]), kr(md["adv_r"])
+    w = float(np.sqrt(E))
+    return dict(tlr=write_specular_rows(w, o["tlr"], kLr, kRa), trl=write_specular_rows(w, o["trl"], kRr, kLa),
+                right=write_specular_rows(w, o["rrr"], kRr, kRa), left=write_specular_rows(w, o["rll"], kLr, kLa),
+                mdl=write_md_rows(w, o["trl"], o["rll"], kRr, kLr, kLa),
+                mdr=write_md_rows(w, o["tlr"], o["rrr"], kLr, kRr, kRa))

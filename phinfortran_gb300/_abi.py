@@ -80,6 +80,17 @@ SIGNATURES = {
                                              C.c_void_p,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_size_t, C.c_void_p]),
+    "pf_transport_tdb_modes_permode_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                     C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                     C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                                     C.c_double, C.c_double, C.c_double,
+                                                     C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int,
+                                                     C.c_void_p,
+                                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                     C.c_void_p, C.c_void_p, C.c_void_p,
+                                                     C.c_void_p, C.c_size_t, C.c_void_p]),
     "pf_tiled_last_error": (C.c_char_p, []),
     "pf_transport_tdb_tiled_workspace_size": (C.c_size_t, [C.c_int] * 7),
     "pf_transport_tdb_tiled_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,

@@ -108,7 +108,15 @@ struct ModeOut {
   double* sums;  // [npts][8]
   int* status;
   int* nprop;    // [npts][4] or null
+  // per-mode outputs (all null, or all set):
+  double* mode_kz;   // [npts][4 problems][mm] k_z of every mode, 100 when not propagating
+  int* mode_bz;      // [npts][4 problems][mm] unfolding label (0: not propagating)
+  double* col_sums;  // [npts][4 matrices][mm columns][nshift] sum of |M_rc|^2 over the rows of each label
+  int mm;            // max(nl, nr)
 };
+
+// reference value of pi (negf/util.f90:5)
+constexpr double kPi = 3.141592653589793238;
 
 __device__ void make_ctx_prep(pf::Ctx<double>& c, const MLayout& lay, char* gscr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -236,7 +244,8 @@ __device__ void mm(int m, int n, int k, pf::Op<double> A, pf::Op<double> B, cons
 
 // One CTA per (point, lead problem).
 __global__ void __launch_bounds__(kTaskThreads)
-    lead_kernel(pf::System<double> sys, pf::Points pts, int p0, int cnt, MLayout lay, Chunk ch, ModeGeom geo) {
+    lead_kernel(pf::System<double> sys, pf::Points pts, int p0, int cnt, MLayout lay, Chunk ch, ModeGeom geo,
+                ModeOut out) {
   const int lp = blockIdx.x >> 2;
   const int kind = blockIdx.x & 3;
   if (lp >= cnt) return;
@@ -312,6 +321,26 @@ __global__ void __launch_bounds__(kTaskThreads)
       bz[t.cols[ci]] = best + 1;
     }
     __syncthreads();
+  }
+  // ---- per-mode outputs in this kernel's mode order: the unfolding label
+  //      and k_z = sign * log_fbz(lambda) (negf/util.f90:825-839; sign -1 on
+  //      the left, velocity_mat.f90:2353-2360), 100 when not propagating
+  if (out.mode_kz) {
+    const size_t o = ((size_t)p * 4 + kind) * out.mm;
+    for (int i = tid; i < m; i += nt) {
+      out.mode_kz[o + i] = 100.0;
+      out.mode_bz[o + i] = bz[i];
+    }
+    __syncthreads();
+    const double az = left ? geo.a_z_l : geo.a_z_r;
+    const double gz = 2.0 * kPi / az;
+    for (int ci = tid; ci < np; ci += nt) {
+      const C lam = t.rowk[ci];
+      double kz = fmod(atan2(lam.y, lam.x) / az, gz);   // Re(log(lambda) / (i a_z)) folded
+      if (kz < 0.0) kz += gz;
+      if (kz > 0.5 * gz) kz -= gz;
+      out.mode_kz[o + t.cols[ci]] = left ? -kz : kz;
+    }
   }
   // ---- velocity matrix V = sign (U^H Gamma U) i a / (2 sqrt(E))
   const C* gam = ch.rec(lp, left ? R_GML : R_GMR);  // Hermitian: Gamma^H == Gamma bitwise
@@ -415,6 +444,30 @@ __global__ void __launch_bounds__(kTaskThreads)
   const int* bz_rr = ch.bz(lp, K_RET_R, lay.m);
   const int* bz_ar = ch.bz(lp, K_ADV_R, lay.m);
   // M = c * Vh_row Uinv_row X Uinv_col Vh_col, X (rows x cols) given as an Op
+  // per-column sums of |M_rc|^2 grouped by the row's label (M in slot 0):
+  // mat 0 tlr, 1 trl, 2 rrr, 3 rll; columns without a label stay zero
+  const int nsh = geo.nshift;
+  auto col_out = [&](int mat, int rows, int cols, const int* bzr, const int* bzc) {
+    if (!out.col_sums) return;
+    double* o = out.col_sums + ((size_t)p * 4 + mat) * out.mm * nsh;
+    for (int u = threadIdx.x; u < cols * nsh; u += blockDim.x) {
+      const int c = u / nsh, b = u % nsh + 1;
+      double acc = 0.0;
+      if (bzc[c] > 0)
+        for (int r = 0; r < rows; ++r)
+          if (bzr[r] == b) {
+            const C e = t.s[0][r + c * ld];
+            acc += e.x * e.x + e.y * e.y;
+          }
+      o[u] = acc;
+    }
+    __syncthreads();
+  };
+  if (out.col_sums) {
+    double* o = out.col_sums + (size_t)p * 4 * out.mm * nsh;
+    for (int u = threadIdx.x; u < 4 * out.mm * nsh; u += blockDim.x) o[u] = 0.0;
+    __syncthreads();
+  }
   auto chain = [&](int rows, int cols, int krow, int kcol, pf::Op<double> X, double cfac) {
     // s0 = Uinv_col Vh_col (cols x cols)
     pf::copy_in(t.s[0], ld, pf::opN<double>(ch.task(lp, kcol, T_UINV), ld), cols, cols);
@@ -438,9 +491,11 @@ __global__ void __launch_bounds__(kTaskThreads)
     // trl = i 2 sqrt(E/azR/azL) Vh_rR Uinv_rR G_D_RL Uinv_aL Vh_aL  -> transr
     chain(nr, nl, K_RET_R, K_ADV_L, pf::opN<double>(ch.rec(lp, R_GDRL), ld), 2.0 * sqrt(E / geo.a_z_r / geo.a_z_l));
     split_sums(t.s[0], ld, nr, nl, bz_rr, bz_al, t.red, &sums[2], &sums[3]);
+    col_out(1, nr, nl, bz_rr, bz_al);
     // tlr = i 2 sqrt(E/azL/azR) Vh_rL Uinv_rL G_D_LR Uinv_aR Vh_aR  -> transl
     chain(nl, nr, K_RET_L, K_ADV_R, pf::opN<double>(ch.rec(lp, R_GDLR), ld), 2.0 * sqrt(E / geo.a_z_l / geo.a_z_r));
     split_sums(t.s[0], ld, nl, nr, bz_rl, bz_ar, t.red, &sums[0], &sums[1]);
+    col_out(0, nl, nr, bz_rl, bz_ar);
     // rrr: (G_R - inv(Q_R)), Q_R = z - Hr - Hrv^H gr Hrv - Hrv grm^H Hrv^H
     bulk_q(t.s[3], t.s[0], t.s[1], t.s[2], ld, nr, E, eps, HR, HRv, pf::opN<double>(ch.rec(lp, R_GRR), ld),
            pf::opC<double>(ch.rec(lp, R_GRM), ld), S);
@@ -456,6 +511,7 @@ __global__ void __launch_bounds__(kTaskThreads)
     // the chain reads X before it reuses slot 3? no: X is copied into s1 first
     chain(nr, nr, K_RET_R, K_ADV_R, pf::opN<double>(t.s[3], ld), 2.0 * sqrt(E / geo.a_z_r / geo.a_z_r));
     split_sums(t.s[0], ld, nr, nr, bz_rr, bz_ar, t.red, &sums[6], &sums[7]);
+    col_out(2, nr, nr, bz_rr, bz_ar);
     // rll: (G_L - inv(Q_L)), Q_L = z - Hl - Hlv^H gl^H Hlv - Hlv glp Hlv^H
     bulk_q(t.s[3], t.s[0], t.s[1], t.s[2], ld, nl, E, eps, HL, HLv, pf::opC<double>(ch.rec(lp, R_GLA), ld),
            pf::opN<double>(ch.rec(lp, R_GLP), ld), S);
@@ -470,6 +526,7 @@ __global__ void __launch_bounds__(kTaskThreads)
     }
     chain(nl, nl, K_RET_L, K_ADV_L, pf::opN<double>(t.s[3], ld), 2.0 * sqrt(E / geo.a_z_l / geo.a_z_l));
     split_sums(t.s[0], ld, nl, nl, bz_rl, bz_al, t.red, &sums[4], &sums[5]);
+    col_out(3, nl, nl, bz_rl, bz_al);
   }
   if (threadIdx.x == 0) {
     for (int k = 0; k < 8; ++k) out.sums[(size_t)p * 8 + k] = sums[k];
@@ -536,14 +593,18 @@ size_t pf_transport_tdb_modes_workspace_size(int n, int nl, int nr, int nq, int 
   return modes_bytes(lay, nq, chunk, grid);
 }
 
-int pf_transport_tdb_modes_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
-                               const double* HR, const double* HRv, const double* Hd, const double* Hdv,
-                               const double* Hld, const double* Hrd, int npts, const double* E, const int* qidx,
-                               const int* zero_flag, double eta, double eta0, double dev_factor, double convergence,
-                               int max_iter, double lambda_eta, double a_z_l, double a_z_r, int nshift,
-                               int stride_l, int nrep_l, const double* phase_l, int stride_r, int nrep_r,
-                               const double* phase_r, double* transl, double* transr, double* mode_sums,
-                               int* status, int* nprop, void* work, size_t work_bytes, void* stream) {
+int pf_transport_tdb_modes_permode_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
+                                       const double* HR, const double* HRv, const double* Hd, const double* Hdv,
+                                       const double* Hld, const double* Hrd, int npts, const double* E,
+                                       const int* qidx, const int* zero_flag, double eta, double eta0,
+                                       double dev_factor, double convergence, int max_iter, double lambda_eta,
+                                       double a_z_l, double a_z_r, int nshift, int stride_l, int nrep_l,
+                                       const double* phase_l, int stride_r, int nrep_r, const double* phase_r,
+                                       double* transl, double* transr, double* mode_sums, int* status, int* nprop,
+                                       double* mode_kz, int* mode_bz, double* col_sums, void* work,
+                                       size_t work_bytes, void* stream) {
+  if ((mode_kz != nullptr) != (mode_bz != nullptr) || (mode_kz != nullptr) != (col_sums != nullptr))
+    return set_err(PF_ERR_ARG, "pf_modes: mode_kz, mode_bz and col_sums are all given or all null");
   if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0)
     return set_err(PF_ERR_ARG, "pf_modes: dimensions must be positive");
   if (n > PF_NMAX_RESIDENT || nl > PF_NMAX_RESIDENT || nr > PF_NMAX_RESIDENT)
@@ -609,7 +670,7 @@ int pf_transport_tdb_modes_dev(int n, int nl, int nr, int L, int nq, const doubl
   geo.nrep_r = nrep_r;
   geo.phase_l = reinterpret_cast<const cx<double>*>(phase_l);
   geo.phase_r = reinterpret_cast<const cx<double>*>(phase_r);
-  ModeOut out{transl, transr, mode_sums, status, nprop};
+  ModeOut out{transl, transr, mode_sums, status, nprop, mode_kz, mode_bz, col_sums, nl > nr ? nl : nr};
   for (int p0 = 0; p0 < npts; p0 += chunk) {
     const int cnt = (npts - p0) < chunk ? (npts - p0) : chunk;
     MD_CUDA(cudaMemsetAsync(queue, 0, sizeof(int), st));
@@ -619,12 +680,27 @@ int pf_transport_tdb_modes_dev(int n, int nl, int nr, int L, int nq, const doubl
     else
       prep_kernel<2><<<g, kPrepThreads, lay.prep_smem, st>>>(sys, pts, p0, cnt, P, lay, ch, gscr, queue, out);
     MD_CUDA(cudaGetLastError());
-    lead_kernel<<<4 * cnt, kTaskThreads, lay.task_smem, st>>>(sys, pts, p0, cnt, lay, ch, geo);
+    lead_kernel<<<4 * cnt, kTaskThreads, lay.task_smem, st>>>(sys, pts, p0, cnt, lay, ch, geo, out);
     MD_CUDA(cudaGetLastError());
     tr_kernel<<<cnt, kTaskThreads, lay.task_smem, st>>>(sys, pts, p0, cnt, lay, ch, geo, eta, eta0, out);
     MD_CUDA(cudaGetLastError());
   }
   return PF_SUCCESS;
+}
+
+int pf_transport_tdb_modes_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
+                               const double* HR, const double* HRv, const double* Hd, const double* Hdv,
+                               const double* Hld, const double* Hrd, int npts, const double* E, const int* qidx,
+                               const int* zero_flag, double eta, double eta0, double dev_factor, double convergence,
+                               int max_iter, double lambda_eta, double a_z_l, double a_z_r, int nshift,
+                               int stride_l, int nrep_l, const double* phase_l, int stride_r, int nrep_r,
+                               const double* phase_r, double* transl, double* transr, double* mode_sums,
+                               int* status, int* nprop, void* work, size_t work_bytes, void* stream) {
+  return pf_transport_tdb_modes_permode_dev(n, nl, nr, L, nq, HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd, npts, E, qidx,
+                                            zero_flag, eta, eta0, dev_factor, convergence, max_iter, lambda_eta,
+                                            a_z_l, a_z_r, nshift, stride_l, nrep_l, phase_l, stride_r, nrep_r,
+                                            phase_r, transl, transr, mode_sums, status, nprop, nullptr, nullptr,
+                                            nullptr, work, work_bytes, stream);
 }
 
 }  // extern "C"

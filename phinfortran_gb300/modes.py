@@ -12,7 +12,11 @@ needs and calls it:
   atoms, latvec_uc = the QE cell; negf/phinfortran.f90:122-160);
 * ``LeadGeometry.phases`` gives, per k point, the unfolding phase of every
   lead orbital for every folded shift (velocity_mat.f90:2035-2072,
-  move_in_ws2 of util.f90:675-706 for the shifted k).
+  move_in_ws2 of util.f90:675-706 for the shifted k);
+* ``mode_rows`` turns the per-mode outputs (``per_mode=True``) into the
+  rows of the reference's per-k mode files (write_specular / write_md,
+  negf/write_data.f90:3-176, called at velocity_mat.f90:3108-3128), which
+  ``output.write_mode_files`` writes.
 """
 from __future__ import annotations
 
@@ -96,6 +100,16 @@ class LeadGeometry:
         n = pos.shape[0]
         return n // self.nshift, 3 * lst.size
 
+    def label_k(self, ksc):
+        """(nshift, 3) Cartesian in-plane k of every unfolding label for the
+        fractional k ``ksc``: move_in_ws2((ksc + shift) . recivec, reci_uc)
+        (velocity_mat.f90:2353-2356; z is replaced by the mode's k_z)."""
+        recivec = 2 * np.pi * np.linalg.inv(self.cell_all).T
+        reci_uc = 2 * np.pi * np.linalg.inv(self.cell_uc).T
+        shifts = [(i, j) for i in range(self.n_bloch[0]) for j in range(self.n_bloch[1])]
+        k = np.asarray(ksc, dtype=np.float64)
+        return np.array([_move_in_ws2((np.array([sx, sy, 0.0]) + k) @ recivec, reci_uc) for sx, sy in shifts])
+
     def phases(self, ksc, side):
         """(nk, nshift, n) complex phases exp(-i(-p.k_sc + (p - p_uc).k_j))."""
         ksc = np.atleast_2d(np.asarray(ksc, dtype=np.float64))
@@ -123,13 +137,15 @@ class LeadGeometry:
 
 
 def transport_tdb_modes(E, blocks, geometry, ksc, *, eta, eta0, convergence, lambda_eta, a_z_l, a_z_r,
-                        dev_factor=10.0, qidx=None, zero_flag=None, max_iter=1000, check=True):
+                        dev_factor=10.0, qidx=None, zero_flag=None, max_iter=1000, check=True, per_mode=False):
     """Transmission and its mode-resolved split for a batch of points.
 
     ``blocks``: one q (dict) or a TdbBlocks stack; ``ksc``: (nq, 3)
     fractional k of every q block (the reference's k_grid rows).  Returns a
     dict with transl, transr, the eight sums of SUM_NAMES, nprop (npts, 4)
-    and status.
+    and status; with ``per_mode`` also mode_kz, mode_bz (npts, 4, mm) and
+    col_sums (npts, 4, mm, nshift) of pf_transport_tdb_modes_permode_dev
+    (problems adv-L, ret-L, ret-R, adv-R; matrices tlr, trl, rrr, rll).
     """
     import torch
     lib = _abi.load()
@@ -159,12 +175,19 @@ def transport_tdb_modes(E, blocks, geometry, ksc, *, eta, eta0, convergence, lam
         raise _abi.PFError(-3, "mode-resolved kernel does not fit (block size > 48?)")
     work = torch.empty(ws, dtype=torch.uint8, device="cuda")
     p = lambda t: None if t is None else t.data_ptr()
-    rc = lib.pf_transport_tdb_modes_dev(n, nl, nr, L, nq, *[dev[k].data_ptr() for k in BLOCK_NAMES], npts,
-                                        Ed.data_ptr(), p(qd), p(zd), eta, eta0, dev_factor, convergence, max_iter,
-                                        lambda_eta, a_z_l, a_z_r, geometry.nshift, sl, rl_, ph_l.data_ptr(), sr, rr_,
-                                        ph_r.data_ptr(), tl.data_ptr(), tr.data_ptr(), sums.data_ptr(), st.data_ptr(),
-                                        npr.data_ptr(), work.data_ptr(), ws,
-                                        C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    args = (n, nl, nr, L, nq, *[dev[k].data_ptr() for k in BLOCK_NAMES], npts, Ed.data_ptr(), p(qd), p(zd), eta,
+            eta0, dev_factor, convergence, max_iter, lambda_eta, a_z_l, a_z_r, geometry.nshift, sl, rl_,
+            ph_l.data_ptr(), sr, rr_, ph_r.data_ptr(), tl.data_ptr(), tr.data_ptr(), sums.data_ptr(), st.data_ptr(),
+            npr.data_ptr())
+    tail = (work.data_ptr(), ws, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if per_mode:
+        mm = max(nl, nr)
+        kz = torch.zeros((max(npts, 1), 4, mm), dtype=torch.float64, device="cuda")
+        bz = torch.zeros((max(npts, 1), 4, mm), dtype=torch.int32, device="cuda")
+        cs = torch.zeros((max(npts, 1), 4, mm, geometry.nshift), dtype=torch.float64, device="cuda")
+        rc = lib.pf_transport_tdb_modes_permode_dev(*args, kz.data_ptr(), bz.data_ptr(), cs.data_ptr(), *tail)
+    else:
+        rc = lib.pf_transport_tdb_modes_dev(*args, *tail)
     if rc != 0:
         raise _abi.PFError(rc, lib.pf_modes_last_error().decode(errors="replace"))
     torch.cuda.synchronize()
@@ -176,4 +199,88 @@ def transport_tdb_modes(E, blocks, geometry, ksc, *, eta, eta0, convergence, lam
                status=status)
     for i, k in enumerate(SUM_NAMES):
         out[k] = s[:, i].copy()
+    if per_mode:
+        out.update(mode_kz=kz.cpu().numpy()[:npts], mode_bz=bz.cpu().numpy()[:npts],
+                   col_sums=cs.cpu().numpy()[:npts], nl=nl, nr=nr)
+    return out
+
+
+KINDS = ("adv_l", "ret_l", "ret_r", "adv_r")
+MATRICES = ("tlr", "trl", "rrr", "rll")
+# write_specular calls (velocity_mat.f90:3108-3120): file -> (matrix, incoming problem)
+SPECULAR_FILES = {"tlr": ("tlr", "adv_r"), "trl": ("trl", "adv_l"), "right": ("rrr", "adv_r"),
+                  "left": ("rll", "adv_l")}
+# write_md calls (velocity_mat.f90:3121-3126): file -> (t matrix, r matrix, incoming problem)
+MD_FILES = {"mdl": ("trl", "rll", "adv_l"), "mdr": ("tlr", "rrr", "adv_r")}
+MODE_FILES = ("left", "right", "tlr", "trl", "mdl", "mdr")
+
+
+def _clamp(x):
+    return 1.0e-60 if 0.0 < x < 1.0e-60 else x
+
+
+def mode_rows(res, geometry, ksc, E, qidx=None):
+    """Rows of the per-k mode files for every point of a per-mode run.
+
+    res: transport_tdb_modes(..., per_mode=True); ksc (nq, 3); E (npts,)
+    energies (omega^2).  Returns {file name: [(q, rows)] per point}, rows a
+    list of tuples (count, omega, k(3), k_pc(3), v_pc(3), sums...) as
+    write_specular (sums r_s, r_t, r_s/r_t) and write_md (sums r_s, r_t,
+    t_s, t_t) write them (negf/write_data.f90:3-176): one row per
+    propagating incoming mode, r_t the sum of |M_ji|^2 over the propagating
+    outgoing modes j and r_s over those whose in-plane k is within 1e-5
+    (squared) of the incoming mode's.  The primitive-cell k and velocity
+    columns (find_k_pc, velocity_mat.f90:2370-2383) are not computed and
+    are written as zero.  Rows follow this library's mode order, which can
+    differ from LAPACK's inside an energy."""
+    ksc = np.atleast_2d(np.asarray(ksc, dtype=np.float64))
+    E = np.asarray(E, dtype=np.float64)
+    npts = E.size
+    q_of = np.zeros(npts, dtype=np.int64) if qidx is None else np.asarray(qidx, dtype=np.int64)
+    nl, nr = res["nl"], res["nr"]
+    size = {"adv_l": nl, "ret_l": nl, "ret_r": nr, "adv_r": nr}
+    labk = [geometry.label_k(k) for k in ksc]
+    out = {name: [] for name in MODE_FILES}
+    zero6 = (0.0,) * 6
+    for p in range(npts):
+        q = int(q_of[p])
+        lk = labk[q]
+        w = float(np.sqrt(E[p]))
+
+        def kvec(kind):
+            ki = KINDS.index(kind)
+            kz, bz = res["mode_kz"][p, ki], res["mode_bz"][p, ki]
+            k = np.full((size[kind], 3), 100.0)
+            for i in range(size[kind]):
+                if kz[i] < 99.9 and bz[i] > 0:
+                    k[i] = lk[bz[i] - 1]
+                    k[i, 2] = kz[i]
+            return k
+
+        def sums(mat, kb, i):
+            S = res["col_sums"][p, MATRICES.index(mat), i]
+            tot = float(np.sum(S))
+            d = lk[:, :2] - kb[i, :2]
+            spec = float(np.sum(S[np.einsum("ij,ij->i", d, d) < 1.0e-5]))
+            return _clamp(spec), _clamp(tot)
+
+        for name, (mat, kind) in SPECULAR_FILES.items():
+            kb = kvec(kind)
+            rows, c = [], 0
+            for i in range(size[kind]):
+                if kb[i, 2] < 99.9:
+                    c += 1
+                    rs, rt = sums(mat, kb, i)
+                    rows.append((c, w, *kb[i], *zero6, rs, rt, rs / rt if rt != 0.0 else 0.0))
+            out[name].append((q, rows))
+        for name, (tmat, rmat, kind) in MD_FILES.items():
+            kb = kvec(kind)
+            rows, c = [], 0
+            for i in range(size[kind]):
+                if kb[i, 2] < 99.9:
+                    c += 1
+                    rs, rt = sums(rmat, kb, i)
+                    ts, tt = sums(tmat, kb, i)
+                    rows.append((c, w, *kb[i], *zero6, rs, rt, ts, tt))
+            out[name].append((q, rows))
     return out

@@ -86,3 +86,31 @@ def read_table(path):
     """(E, T) of a table written by the reference or by write_trans."""
     a = np.loadtxt(path, ndmin=2)
     return a[:, 0], a[:, 1:]
+
+
+def mode_file_line(row):
+    """One row of a per-k mode file: count in I5, then the values in
+    Fortran E20.10 (formats 1000 of negf/write_data.f90:69 and :171)."""
+    return f"{int(row[0]):5d}" + "".join(fortran_e(v, 20, 10) for v in row[1:]) + "\n"
+
+
+def write_mode_files(output_dir, rows, k_index=None):
+    """Append the per-k mode files ``{name}_specular_param_{k:06d}.dat``
+    (negf/write_data.f90:3-176) for the rows of ``modes.mode_rows``.
+
+    ``rows``: {name: [(q, rows)] in point order}; ``k_index`` maps q to the
+    reference's 1-based k number (default q + 1).  Like the reference the
+    files are opened for appending, so points are written in the order
+    given (energy order for one k) and an existing file grows."""
+    os.makedirs(output_dir, exist_ok=True)
+    for name, per_point in rows.items():
+        files = {}
+        try:
+            for q, rr in per_point:
+                k = (k_index[q] if k_index is not None else q + 1)
+                if k not in files:
+                    files[k] = open(os.path.join(output_dir, f"{name}_specular_param_{int(k):06d}.dat"), "a")
+                files[k].writelines(mode_file_line(r) for r in rr)
+        finally:
+            for f in files.values():
+                f.close()

@@ -9,8 +9,10 @@ examples/negf/si-si (read by the oracle's restatement of negf/fc.f90), and
 (b) the reference's own committed outputs output/trans{l,r}_tot.dat,
 trans{l,r}_{s,ns}.dat and refl{l,r}_{s,ns}.dat (61 omega^2 x 49 k), so the
 GPU tests can check parity on a machine without the reference checkout;
-and tests/golden/sisi_output_head.txt, the first rows of those tables
-verbatim, which pin the text format of the output writer.
+tests/golden/sisi_output_head.txt, the first rows of those tables
+verbatim, which pin the text format of the output writer; and
+tests/golden/sisi_perk.npz / sisi_perk_head.txt, the per-k mode files
+(output/*_specular_param_*.dat) of three k points.
 """
 from __future__ import annotations
 
@@ -70,6 +72,30 @@ def text_heads(out=os.path.join(HERE, "sisi_output_head.txt"), nlines=3):
     print("wrote", out)
 
 
+PERK_FILES = ["left", "right", "tlr", "trl", "mdl", "mdr"]
+PERK_K = [0, 10, 37]   # 0-based k indices whose per-k mode files are kept
+
+
+def perk(out=os.path.join(HERE, "sisi_perk.npz"), head=os.path.join(HERE, "sisi_perk_head.txt"), nlines=3):
+    """The reference's per-k mode files (negf/write_data.f90:3-176) of a few
+    k points, parsed (rows of count, E, k, k_pc, v_pc, sums), and the first
+    rows of the k = 1 files verbatim (their text format)."""
+    arrs = {}
+    with open(head, "w") as h:
+        for name in PERK_FILES:
+            for ik in PERK_K:
+                path = os.path.join(REF, "output", f"{name}_specular_param_{ik + 1:06d}.dat")
+                arrs[f"{name}_{ik}"] = np.loadtxt(path, ndmin=2)
+                if ik == 0:
+                    with open(path) as g:
+                        rows = [next(g) for _ in range(nlines)]
+                    h.write(f"# {name}\n")
+                    h.writelines(rows)
+    np.savez_compressed(out, k_index=np.array(PERK_K), **arrs)
+    print("wrote", out, head)
+
+
 if __name__ == "__main__":
     main()
     text_heads()
+    perk()

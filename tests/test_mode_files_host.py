@@ -1,0 +1,94 @@
+"""The reference's per-k mode files (write_specular / write_md,
+negf/write_data.f90:3-176, called at negf/velocity_mat.f90:3108-3128), CPU
+side: the text format of the writer against the reference's own lines, the
+oracle's rows against the reference's files of three k points, and the
+append behaviour of the writer."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import modes as M
+from phinfortran_gb300.output import mode_file_line, write_mode_files
+from tests.test_modes_host import oracle_point_sums
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FILES = ("left", "right", "tlr", "trl", "mdl", "mdr")
+
+
+@pytest.fixture(scope="module")
+def perk():
+    return np.load(os.path.join(HERE, "golden", "sisi_perk.npz"))
+
+
+def compare_rows(A, B, md):
+    """Rows of one file against the reference's: the same energies, per
+    energy the same number of rows and (after sorting by k, since the
+    mode order inside an energy follows the eigen-solver) the same k within
+    2e-9 (10-digit output), the sums within 5e-7 relative + 1e-12, the
+    ratio r_s/r_t within 1e-9 where r_t > 1e-8 (below that it is the ratio
+    of two rounding-level reflections).  Columns 6-11 (primitive-cell k and
+    velocity) are not compared."""
+    A, B = np.asarray(A, dtype=np.float64), np.asarray(B, dtype=np.float64)
+
+    def groups(a):
+        d = {}
+        for r in a:
+            d.setdefault(round(float(r[1]), 8), []).append(r)
+        return d
+
+    ga, gb = groups(A), groups(B)
+    assert sorted(ga) == sorted(gb)
+    cols = [11, 12, 13, 14] if md else [11, 12]
+    for e, rb in gb.items():
+        key = lambda r: tuple(np.round(r[2:5], 6))
+        a, b = np.array(sorted(ga[e], key=key)), np.array(sorted(rb, key=key))
+        assert a.shape == b.shape, e
+        assert sorted(a[:, 0]) == list(range(1, a.shape[0] + 1)), e
+        assert np.abs(a[:, 2:5] - b[:, 2:5]).max() <= 2e-9, e
+        assert (np.abs(a[:, cols] - b[:, cols]) <= 5e-7 * np.abs(b[:, cols]) + 1e-12).all(), e
+        if not md:
+            m = b[:, 12] > 1e-8
+            assert (np.abs(a[m, 13] - b[m, 13]) <= 1e-9).all(), e
+
+
+def test_mode_file_line_matches_reference_text(perk):
+    """Format 1000 of write_specular / write_md: I5 then E20.10."""
+    with open(os.path.join(HERE, "golden", "sisi_perk_head.txt")) as f:
+        text = f.read().split("# ")[1:]
+    assert len(text) == len(FILES)
+    for block in text:
+        name, *lines = block.rstrip("\n").split("\n")
+        rows = perk[f"{name}_0"]
+        for i, line in enumerate(lines):
+            assert mode_file_line(rows[i]) == line + "\n", (name, i)
+
+
+@pytest.mark.parametrize("ik", [0, 37])
+def test_oracle_mode_rows_match_reference(sisi, perk, ik):
+    f = sisi
+    cell = f["cell"]
+    nb = tuple(int(x) for x in f["n_bloch"])
+    reci_uc = 2 * np.pi * np.linalg.inv(cell).T
+    geom = dict(ksc=f["kgrid"][ik], recivec=2 * np.pi * np.linalg.inv(f["cell_all"]).T, reci_uc_l=reci_uc,
+                reci_uc_r=reci_uc, nb=nb)
+    rows = {n: [] for n in FILES}
+    for ie, (o, _) in enumerate(oracle_point_sums(f, ik, list(range(f["E"].size)))):
+        for n, rr in M.mode_file_rows(f["E"][ie], o, geom).items():
+            rows[n] += rr
+    for n in FILES:
+        compare_rows(rows[n], perk[f"{n}_{ik}"], n.startswith("md"))
+
+
+def test_write_mode_files_appends_in_order(tmp_path, perk):
+    """The reference opens the files with POSITION='APPEND': two calls for
+    the same k extend one file; names carry the 1-based k number."""
+    rows = perk["left_0"]
+    first = [tuple(r) for r in rows[:3]]
+    second = [tuple(r) for r in rows[3:5]]
+    write_mode_files(str(tmp_path), {"left": [(0, first)]})
+    write_mode_files(str(tmp_path), {"left": [(0, second)], "mdl": [(4, [])]}, k_index={0: 1, 4: 12})
+    path = tmp_path / "left_specular_param_000001.dat"
+    back = np.loadtxt(path, ndmin=2)
+    np.testing.assert_allclose(back, rows[:5], rtol=1e-9, atol=0)
+    assert (tmp_path / "mdl_specular_param_000012.dat").exists()
