@@ -63,7 +63,8 @@ def main():
     ap.add_argument("--width", type=int, default=0)
     ap.add_argument("--nc", type=int, default=2)
     ap.add_argument("--perturb", type=float, default=0.0)
-    ap.add_argument("--out", default="", help="sisi: write the reference's ten output tables into this directory")
+    ap.add_argument("--out", default="",
+                    help="sisi: write the reference's ten output tables and the per-k mode files into this directory")
     a = ap.parse_args()
     import torch
     out = dict(workload=a.workload, mode=a.mode)
@@ -93,16 +94,19 @@ def main():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         r = transport_tdb_modes(E, blocks, geo, f["kgrid"][ks], qidx=q, zero_flag=zf, lambda_eta=5e-3,
-                                a_z_l=f["cell"][2, 2],
-                                a_z_r=f["cell"][2, 2], check=False, **p)
+                                a_z_l=f["cell"][2, 2], a_z_r=f["cell"][2, 2], check=False,
+                                per_mode=bool(a.out), **p)
         torch.cuda.synchronize()
         out.update(points=int(E.size), seconds=time.perf_counter() - t0, transl=r["transl"].tolist(),
                    transl_s=r["transl_s"].tolist(), status=int(np.bitwise_or.reduce(r["status"])))
         if a.out:
-            from .modes import SUM_NAMES
-            from .output import write_trans
+            from .modes import SUM_NAMES, mode_rows
+            from .output import write_mode_files, write_trans
             grid = lambda v: np.asarray(v).reshape(len(ks), E1.size).T      # (ne, nk) as the reference
             write_trans(a.out, E1, grid(r["transl"]), grid(r["transr"]), **{k: grid(r[k]) for k in SUM_NAMES})
+            # the per-k mode files, numbered by the k's place in the 49-point grid
+            write_mode_files(a.out, mode_rows(r, geo, f["kgrid"][ks], E, qidx=q),
+                             k_index={i: k + 1 for i, k in enumerate(ks)})
             out["written"] = a.out
         print(json.dumps(out))
         return
