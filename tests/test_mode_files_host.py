@@ -92,3 +92,50 @@ def test_write_mode_files_appends_in_order(tmp_path, perk):
     back = np.loadtxt(path, ndmin=2)
     np.testing.assert_allclose(back, rows[:5], rtol=1e-9, atol=0)
     assert (tmp_path / "mdl_specular_param_000012.dat").exists()
+
+
+def test_mode_rows_assembly_matches_oracle_rows(sisi):
+    """modes.mode_rows (the host half of the per-k files) fed with per-mode
+    data built from the oracle's matrices -- k_z, labels and the per-label
+    column sums the GPU entry returns -- gives the oracle's rows exactly,
+    mode order included."""
+    from phinfortran_gb300.modes import KINDS, MATRICES, LeadGeometry, mode_rows
+
+    f = sisi
+    ik, ies = 37, [5, 11, 25, 50]
+    nb = tuple(int(x) for x in f["n_bloch"])
+    b, p = int(f["buffer"]), int(f["period"])
+    geo = LeadGeometry.from_qe(f["pos_all"], f["cell"], f["cell_all"], nb, b, p, b, p)
+    cell = f["cell"]
+    reci_uc = 2 * np.pi * np.linalg.inv(cell).T
+    geom = dict(ksc=f["kgrid"][ik], recivec=2 * np.pi * np.linalg.inv(f["cell_all"]).T, reci_uc_l=reci_uc,
+                reci_uc_r=reci_uc, nb=nb)
+    pts = oracle_point_sums(f, ik, ies)
+    nl = pts[0][0]["rll"].shape[0]
+    nr = pts[0][0]["rrr"].shape[0]
+    mm, ns = max(nl, nr), nb[0] * nb[1]
+    res = dict(mode_kz=np.zeros((len(ies), 4, mm)), mode_bz=np.zeros((len(ies), 4, mm), np.int32),
+               col_sums=np.zeros((len(ies), 4, mm, ns)), nl=nl, nr=nr)
+    rows_of = {"tlr": ("ret_l", "adv_r"), "trl": ("ret_r", "adv_l"), "rrr": ("ret_r", "adv_r"),
+               "rll": ("ret_l", "adv_l")}
+    for a, (o, _) in enumerate(pts):
+        md = o["modes"]
+        for ki, kind in enumerate(KINDS):
+            m = md[kind]
+            res["mode_kz"][a, ki, :m["kz"].size] = m["kz"]
+            res["mode_bz"][a, ki, :m["bz"].size] = m["bz"]
+        for mi, mat in enumerate(MATRICES):
+            M2 = np.abs(o[mat]) ** 2
+            br, bc = md[rows_of[mat][0]]["bz"], md[rows_of[mat][1]]["bz"]
+            for c in range(M2.shape[1]):
+                if bc[c] > 0:
+                    for lab in range(1, ns + 1):
+                        res["col_sums"][a, mi, c, lab - 1] = M2[br == lab, c].sum()
+    E = f["E"][ies]
+    got = mode_rows(res, geo, f["kgrid"][[ik]], E)
+    for a, (o, _) in enumerate(pts):
+        want = M.mode_file_rows(E[a], o, geom)
+        for name in FILES:
+            g = np.array(got[name][a][1], dtype=np.float64).reshape(-1, 15 if name.startswith("md") else 14)
+            w = np.array(want[name], dtype=np.float64).reshape(g.shape)
+            np.testing.assert_allclose(g, w, rtol=1e-12, atol=1e-300, err_msg=f"{name} point {a}")
