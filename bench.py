@@ -12,8 +12,9 @@ T(E) per (E, q) point ("solve").
     python bench.py --impl reference ...   (CPU oracle on the host cores)
 
 Rank 0 prints one JSON line.  `value` = solves/s of the headline path
-(default: mixed precision -- double-float leads, FP32 factorisation, one
-double-float refinement sweep) with inputs resident in HBM (CUDA events
+(default: mixed precision -- double-float leads, FP32 factorisation,
+double-float refinement: one sweep for every point and a second for the
+points whose first correction was above 3e-5) with inputs resident in HBM (CUDA events
 around each step on the launching stream, L2 flushed before every step);
 `e2e` = the same through the host-pointer C entry with host buffers, copies
 inside the timed region; `compare` = the plain FP64 path on the same batch
@@ -419,8 +420,8 @@ def main():
                     "on the FP32 pipe (FP32 and double-float arithmetic); achieved counts the FP64-equivalent "
                     "algorithmic flops F(n,L,I) per step only")
         kernel = ("mixed pipeline per step: leads_kernel (double-float decimation, CTA per point) + layer_kernel "
-                  "(warp per point: FP32 LU, back substitution, refinement corrections, Caroli) + residual_kernel; "
-                  "achieved = F per step / step time")
+                  "(warp per point: FP32 LU, back substitution, refinement corrections, Caroli; the adaptive second "
+                  "sweep with a CTA per listed point) + residual_kernel; achieved = F per step / step time")
     roof = dict(bound="tensor", achieved=achieved, peak=peak, unit="TFLOP/s", frac=achieved / peak, traffic=None,
                 peak_source=peak_src, kernel=kernel, algorithmic_flops_per_launch=fl,
                 flops_formula="n^3 (40 L + 16) + 2 n^3 (56 I + 24)", mean_decimation_iters=iters)
