@@ -281,11 +281,18 @@ __device__ int adjoint_point_ckpt(const Ctx<R>& c, const System<R>& sys, int q, 
   cx<R>* s1 = c.sm[1];
   cx<R>* s2 = c.sm[2];
   cx<R>* s3 = c.sm[3];
-  // ---- pass A
+  // ---- pass A; the last segment's factors and y vectors go straight into
+  //      the segment buffer, so pass B does not recompute that segment
+  const int nseg = (L + 2 + seg - 1) / seg;
+  const int cl = (nseg - 1) * seg;  // first layer of the last segment
   copy_in(sl.pg, ld, opN<R>(c.gs[G_GL], ld), nl, nl);
   copy_in(sl.py, ld, opC<R>(c.gs[G_GL], ld), nl, nl);
   copy_in(sl.ckg, ld, opN<R>(c.gs[G_GL], ld), nl, nl);
   copy_in(sl.cky, ld, opC<R>(c.gs[G_GL], ld), nl, nl);
+  if (cl == 0) {
+    copy_in(sl.segg, ld, opN<R>(c.gs[G_GL], ld), nl, nl);
+    copy_in(sl.segy, ld, opC<R>(c.gs[G_GL], ld), nl, nl);
+  }
   for (int j = 1; j <= L + 1; ++j) {
     const int dj = xdim(sys, j);
     // s0 = V_{j-1}, s1 = scratch, s2 = g_j; y_j -> py (its product reads s1, not py)
@@ -295,6 +302,10 @@ __device__ int adjoint_point_ckpt(const Ctx<R>& c, const System<R>& sys, int q, 
     if (j % seg == 0) {
       copy_out(sl.ckg + (size_t)(j / seg) * mat, ld, false, s2, ld, dj, dj);
       copy_out(sl.cky + (size_t)(j / seg) * mat, ld, false, s3, ld, dj, nl);
+    }
+    if (j >= cl) {
+      copy_out(sl.segg + (size_t)(j - cl) * mat, ld, false, s2, ld, dj, dj);
+      copy_out(sl.segy + (size_t)(j - cl) * mat, ld, false, s3, ld, dj, nl);
     }
   }
   // ---- T and W from X_0 = G^L_{0,L+1} = y_{L+1}^H (py holds y_{L+1}, nr x nl)
@@ -312,17 +323,19 @@ __device__ int adjoint_point_ckpt(const Ctx<R>& c, const System<R>& sys, int q, 
   cx<R>* xn = sl.xb;
   cx<R>* kc = sl.k0;
   cx<R>* kn = sl.k1;
-  const int nseg = (L + 2 + seg - 1) / seg;
   for (int k = nseg - 1; k >= 0; --k) {
     const int c0 = k * seg;
     const int e = (c0 + seg < L + 2) ? c0 + seg : L + 2;
-    // recompute the segment's factors and y vectors (slots: s1, s2 and the free Z slot)
-    copy_in(sl.segg, ld, opN<R>(sl.ckg + (size_t)k * mat, ld), xdim(sys, c0), xdim(sys, c0));
-    copy_in(sl.segy, ld, opN<R>(sl.cky + (size_t)k * mat, ld), xdim(sys, c0), nl);
-    for (int j = c0 + 1; j < e; ++j) {
-      const int i = j - c0;
-      st |= ckpt_step<R, S>(c, sys, q, zD, j, sl.segg + (size_t)(i - 1) * mat, sl.segy + (size_t)(i - 1) * mat, s1, s2,
-                         sZ, sl.segg + (size_t)i * mat, sl.segy + (size_t)i * mat);
+    // recompute the segment's factors and y vectors (slots: s1, s2 and the
+    // free Z slot); the last segment is still in the buffer from pass A
+    if (k < nseg - 1) {
+      copy_in(sl.segg, ld, opN<R>(sl.ckg + (size_t)k * mat, ld), xdim(sys, c0), xdim(sys, c0));
+      copy_in(sl.segy, ld, opN<R>(sl.cky + (size_t)k * mat, ld), xdim(sys, c0), nl);
+      for (int j = c0 + 1; j < e; ++j) {
+        const int i = j - c0;
+        st |= ckpt_step<R, S>(c, sys, q, zD, j, sl.segg + (size_t)(i - 1) * mat, sl.segy + (size_t)(i - 1) * mat,
+                              s1, s2, sZ, sl.segg + (size_t)i * mat, sl.segy + (size_t)i * mat);
+      }
     }
     // W is the right operand of every K_j of the segment: keep it in the
     // shared slot the recomputation used as scratch

@@ -16,11 +16,13 @@ def small_bar(seed=4):
     return S.sc_phonon(nx=2, ny=2, L=5, ne=16, mass_range=(1, 3), bond_range=(0.8, 1.2), seed_index=seed)
 
 
-@pytest.mark.parametrize("ckpt,arith", [(1, "fp64"), (0, "fp64"), (3, "fp64"), (1, "df64"), (0, "df64")])
+@pytest.mark.parametrize("ckpt,arith", [(1, "fp64"), (0, "fp64"), (3, "fp64"), (7, "fp64"), (1, "df64"),
+                                        (0, "df64"), (2, "df64")])
 def test_sensitivities_match_oracle(cuda_ready, ckpt, arith):
     """ckpt = 1 keeps every layer; 0 checkpoints every ceil(sqrt(L+2)) = 3
-    layers and recomputes; 3 with L = 5 leaves a short last segment.
-    df64: every block operation in double-float (about 48 bits)."""
+    layers and recomputes; 3 with L = 5 leaves a short last segment; 7 is
+    one segment (kept from the forward pass, nothing recomputed); 2 four
+    segments.  df64: every block operation in double-float (about 48 bits)."""
     b, E, p, aux = small_bar()
     Es = E[2:14]
     w = np.linspace(0.3, 1.7, Es.size)
