@@ -24,6 +24,10 @@ def test_fixture_regenerates_from_reference(sisi):
     assert np.array_equal(qe["fc"], sisi["fc"])
     g = np.loadtxt(os.path.join(REF, "output", "transl_tot.dat"))
     assert np.array_equal(g[:, 1:], sisi["transl_tot"])
+    perk = np.load(os.path.join(os.path.dirname(__file__), "golden", "sisi_perk.npz"))
+    for ik in perk["k_index"]:
+        g = np.loadtxt(os.path.join(REF, "output", f"mdl_specular_param_{int(ik) + 1:06d}.dat"), ndmin=2)
+        assert np.array_equal(g, perk[f"mdl_{int(ik)}"])
 
 
 def test_energy_and_k_grids(sisi):
