@@ -249,39 +249,56 @@ def _spec_sums(r, kf, kb, i):
     return rs, rt
 
 
-def write_specular_rows(w, r, kf, kb):
-    """negf/write_data.f90:3-76 (k_pc and v_pc columns as zero)."""
+def write_specular_rows(w, r, kf, kb, pcb=None):
+    """negf/write_data.f90:3-76; pcb (nb, 6): k_pc and v_pc of the incoming
+    modes (zero when None)."""
+    pcb = np.zeros((kb.shape[0], 6)) if pcb is None else pcb
     rows, c = [], 0
     for i in range(kb.shape[0]):
         if kb[i, 2] < 99.9:
             c += 1
             rs, rt = _spec_sums(r, kf, kb, i)
-            rows.append((c, w, *kb[i], *(0.0,) * 6, rs, rt, rs / rt if rt != 0.0 else 0.0))
+            rows.append((c, w, *kb[i], *pcb[i], rs, rt, rs / rt if rt != 0.0 else 0.0))
     return rows
 
 
-def write_md_rows(w, t, r, kft, kf, kb):
-    """negf/write_data.f90:78-176 (k_pc and v_pc columns as zero)."""
+def write_md_rows(w, t, r, kft, kf, kb, pcb=None):
+    """negf/write_data.f90:78-176; pcb as in write_specular_rows."""
+    pcb = np.zeros((kb.shape[0], 6)) if pcb is None else pcb
     rows, c = [], 0
     for i in range(kb.shape[0]):
         if kb[i, 2] < 99.9:
             c += 1
             rs, rt = _spec_sums(r, kf, kb, i)
             ts, tt = _spec_sums(t, kft, kb, i)
-            rows.append((c, w, *kb[i], *(0.0,) * 6, rs, rt, ts, tt))
+            rows.append((c, w, *kb[i], *pcb[i], rs, rt, ts, tt))
     return rows
 
 
-def mode_file_rows(E, o, geom):
+def mode_file_rows(E, o, geom, find_pc=None):
     """Rows of the six per-k files for one point of vel_mat_tdb
-    (velocity_mat.f90:3108-3128)."""
+    (velocity_mat.f90:3108-3128).  find_pc(E, k) -> (k_pc, v_pc) gives the
+    primitive-cell columns (oracle/unfold_pc.find_k_pc; zero when None)."""
     g = geom
     md = o["modes"]
     kl = lambda m: k_xyz(m, g["ksc"], g["recivec"], g["reci_uc_l"], g["nb"])
     kr = lambda m: k_xyz(m, g["ksc"], g["recivec"], g["reci_uc_r"], g["nb"])
     kLr, kLa, kRr, kRa = kl(md["ret_l"]), kl(md["adv_l"]), kr(md["ret_r"]), kr(md["adv_r"])
+
+    def pcols(kb):
+        out = np.zeros((kb.shape[0], 6))
+        if find_pc is not None:
+            for i in range(kb.shape[0]):
+                if kb[i, 2] < 99.9:
+                    kp, vp = find_pc(E, kb[i])
+                    out[i, :3], out[i, 3:] = kp, vp
+        return out
+
+    pLa, pRa = pcols(kLa), pcols(kRa)
     w = float(np.sqrt(E))
-    return dict(tlr=write_specular_rows(w, o["tlr"], kLr, kRa), trl=write_specular_rows(w, o["trl"], kRr, kLa),
-                right=write_specular_rows(w, o["rrr"], kRr, kRa), left=write_specular_rows(w, o["rll"], kLr, kLa),
-                mdl=write_md_rows(w, o["trl"], o["rll"], kRr, kLr, kLa),
-                mdr=write_md_rows(w, o["tlr"], o["rrr"], kLr, kRr, kRa))
+    return dict(tlr=write_specular_rows(w, o["tlr"], kLr, kRa, pRa),
+                trl=write_specular_rows(w, o["trl"], kRr, kLa, pLa),
+                right=write_specular_rows(w, o["rrr"], kRr, kRa, pRa),
+                left=write_specular_rows(w, o["rll"], kLr, kLa, pLa),
+                mdl=write_md_rows(w, o["trl"], o["rll"], kRr, kLr, kLa, pLa),
+                mdr=write_md_rows(w, o["tlr"], o["rrr"], kLr, kRr, kRa, pRa))

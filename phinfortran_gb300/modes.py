@@ -219,7 +219,7 @@ def _clamp(x):
     return 1.0e-60 if 0.0 < x < 1.0e-60 else x
 
 
-def mode_rows(res, geometry, ksc, E, qidx=None):
+def mode_rows(res, geometry, ksc, E, qidx=None, pc=None):
     """Rows of the per-k mode files for every point of a per-mode run.
 
     res: transport_tdb_modes(..., per_mode=True); ksc (nq, 3); E (npts,)
@@ -230,8 +230,9 @@ def mode_rows(res, geometry, ksc, E, qidx=None):
     propagating incoming mode, r_t the sum of |M_ji|^2 over the propagating
     outgoing modes j and r_s over those whose in-plane k is within 1e-5
     (squared) of the incoming mode's.  The primitive-cell k and velocity
-    columns (find_k_pc, velocity_mat.f90:2370-2383) are not computed and
-    are written as zero.  Rows follow this library's mode order, which can
+    columns (find_k_pc, velocity_mat.f90:2370-2383) come from ``pc``, an
+    ``unfold_pc.PrimitiveCell`` (both leads) or a (left, right) pair, and
+    are zero without it.  Rows follow this library's mode order, which can
     differ from LAPACK's inside an energy."""
     ksc = np.atleast_2d(np.asarray(ksc, dtype=np.float64))
     E = np.asarray(E, dtype=np.float64)
@@ -241,7 +242,7 @@ def mode_rows(res, geometry, ksc, E, qidx=None):
     size = {"adv_l": nl, "ret_l": nl, "ret_r": nr, "adv_r": nr}
     labk = [geometry.label_k(k) for k in ksc]
     out = {name: [] for name in MODE_FILES}
-    zero6 = (0.0,) * 6
+    pcs = (pc, pc) if pc is None or not isinstance(pc, (tuple, list)) else tuple(pc)
     for p in range(npts):
         q = int(q_of[p])
         lk = labk[q]
@@ -264,23 +265,33 @@ def mode_rows(res, geometry, ksc, E, qidx=None):
             spec = float(np.sum(S[np.einsum("ij,ij->i", d, d) < 1.0e-5]))
             return _clamp(spec), _clamp(tot)
 
-        for name, (mat, kind) in SPECULAR_FILES.items():
+        # incoming modes of each side with their primitive-cell columns
+        inc = {}
+        for kind, side in (("adv_l", 0), ("adv_r", 1)):
             kb = kvec(kind)
+            pcols = np.zeros((size[kind], 6))
+            prop = np.nonzero(kb[:, 2] < 99.9)[0]
+            if pcs[side] is not None and prop.size:
+                kp, vp = pcs[side].unfold(E[p], kb[prop])
+                pcols[prop, :3], pcols[prop, 3:] = kp, vp
+            inc[kind] = (kb, pcols)
+        for name, (mat, kind) in SPECULAR_FILES.items():
+            kb, pcols = inc[kind]
             rows, c = [], 0
             for i in range(size[kind]):
                 if kb[i, 2] < 99.9:
                     c += 1
                     rs, rt = sums(mat, kb, i)
-                    rows.append((c, w, *kb[i], *zero6, rs, rt, rs / rt if rt != 0.0 else 0.0))
+                    rows.append((c, w, *kb[i], *pcols[i], rs, rt, rs / rt if rt != 0.0 else 0.0))
             out[name].append((q, rows))
         for name, (tmat, rmat, kind) in MD_FILES.items():
-            kb = kvec(kind)
+            kb, pcols = inc[kind]
             rows, c = [], 0
             for i in range(size[kind]):
                 if kb[i, 2] < 99.9:
                     c += 1
                     rs, rt = sums(rmat, kb, i)
                     ts, tt = sums(tmat, kb, i)
-                    rows.append((c, w, *kb[i], *zero6, rs, rt, ts, tt))
+                    rows.append((c, w, *kb[i], *pcols[i], rs, rt, ts, tt))
             out[name].append((q, rows))
     return out

@@ -104,8 +104,13 @@ def main():
             from .output import write_mode_files, write_trans
             grid = lambda v: np.asarray(v).reshape(len(ks), E1.size).T      # (ne, nk) as the reference
             write_trans(a.out, E1, grid(r["transl"]), grid(r["transr"]), **{k: grid(r[k]) for k in SUM_NAMES})
-            # the per-k mode files, numbered by the k's place in the 49-point grid
-            write_mode_files(a.out, mode_rows(r, geo, f["kgrid"][ks], E, qidx=q),
+            # the per-k mode files, numbered by the k's place in the 49-point grid,
+            # with the primitive-cell columns of pc1.fdf (both leads)
+            from .unfold_pc import PrimitiveCell
+            qe = dict(pos=f["pos"], cell=f["cell"], fc=f["fc"], rws=f["rws"], rd=f["rd"], nxyz=f["nxyz"])
+            pc = PrimitiveCell(qe, f["pc_latvec"], f["pc_scaled"], f["pc_species"], float(f["pc_lscale"]),
+                               f["mass_no"], 2 * np.pi * np.linalg.inv(f["cell"]).T, max(nb))
+            write_mode_files(a.out, mode_rows(r, geo, f["kgrid"][ks], E, qidx=q, pc=pc),
                              k_index={i: k + 1 for i, k in enumerate(ks)})
             out["written"] = a.out
         print(json.dumps(out))

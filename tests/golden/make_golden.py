@@ -6,7 +6,8 @@ Run in a checkout that has the reference at /root/reference:
 
 The fixture holds (a) the processed force constants and supercell of
 examples/negf/si-si (read by the oracle's restatement of negf/fc.f90), and
-(b) the reference's own committed outputs output/trans{l,r}_tot.dat,
+(b) the primitive-cell input pc1.fdf and the species masses, (c) the
+reference's own committed outputs output/trans{l,r}_tot.dat,
 trans{l,r}_{s,ns}.dat and refl{l,r}_{s,ns}.dat (61 omega^2 x 49 k), so the
 GPU tests can check parity on a machine without the reference checkout;
 tests/golden/sisi_output_head.txt, the first rows of those tables
@@ -44,6 +45,20 @@ def main(out=os.path.join(HERE, "sisi.npz")):
         gold[name] = a[:, 1:]
         gold["E_" + name] = a[:, 0]
     r_table = np.loadtxt(os.path.join(REF, "fc_qe_r.dat"))
+    # primitive-cell input of both leads (config: left/right_primitive_cell_input = pc1.fdf)
+    pc = {}
+    with open(os.path.join(REF, "pc1.fdf")) as g:
+        lines = g.read().splitlines()
+    for i, line in enumerate(lines):
+        if line.startswith("LatticeConstant"):
+            pc["pc_lscale"] = float(line.split()[1])
+        if "%block LatticeVectors" in line:
+            pc["pc_latvec"] = np.array([[float(x) for x in lines[i + 1 + r].split()] for r in range(3)])
+        if "%block AtomicScaledCoordinatesAndAtomicSpecies" in line:
+            rows = [lines[i + 1 + r].split() for r in range(4)]
+            pc["pc_scaled"] = np.array([[float(x) for x in r[:3]] for r in rows])
+            pc["pc_species"] = np.array([int(r[3]) for r in rows])
+    mass_no_all = Q.read_species_masses(os.path.join(REF, "trans_input.fdf"))
     np.savez_compressed(
         out, fc=qe["fc"], cell=qe["cell"], pos=qe["pos"], mass=qe["mass"],
         nxyz=np.array([qe["nx"], qe["ny"], qe["nz"]]), cell_sc=qe["cell_sc"], rws=qe["rws"], rd=qe["rd"],
@@ -52,7 +67,7 @@ def main(out=os.path.join(HERE, "sisi.npz")):
         # config of examples/negf/si-si/config
         eta=1.0e-8, eta0=1.0e-9, convergence=1.17e-14, dev_factor=10.0,
         n_bloch=np.array([2, 2]), nz=8, buffer=16, period=16, nlayer=2, natm_layer=16,
-        **gold)
+        mass_no=mass_no_all, **pc, **gold)
     print("wrote", out)
 
 

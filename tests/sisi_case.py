@@ -62,3 +62,28 @@ def fp64_noise_floor(E, blocks, params, trials=3, rel=1e-15, seed=11):
         o = N.transport(E, bp, params["eta"], params["eta0"], params["convergence"], params["dev_factor"])
         dev = np.maximum(dev, np.abs(o["transl"] - base["transl"]))
     return base, dev
+
+
+def sisi_qe(f):
+    """The processed QE force constants of the fixture as the primitive-cell
+    unfolding takes them."""
+    return dict(pos=f["pos"], cell=f["cell"], fc=f["fc"], rws=f["rws"], rd=f["rd"], nxyz=f["nxyz"])
+
+
+def sisi_primitive_cell(f):
+    """unfold_pc.PrimitiveCell of the si-si leads (pc1.fdf on both sides)."""
+    from phinfortran_gb300.unfold_pc import PrimitiveCell
+    nb = f["n_bloch"]
+    return PrimitiveCell(sisi_qe(f), f["pc_latvec"], f["pc_scaled"], f["pc_species"], float(f["pc_lscale"]),
+                         f["mass_no"], 2 * np.pi * np.linalg.inv(f["cell"]).T, int(max(nb[0], nb[1])))
+
+
+def sisi_find_pc(f):
+    """The oracle's find_k_pc for the si-si leads, as find_pc(E, k)."""
+    from oracle import unfold_pc as U
+    pos_pc, rec_pc, mass_uc = U.primitive_cell(f["pc_latvec"], f["pc_scaled"], f["pc_species"],
+                                               float(f["pc_lscale"]), f["mass_no"])
+    dyn = U.PcDyn(sisi_qe(f), pos_pc.shape[0], mass_uc)
+    reci_uc = 2 * np.pi * np.linalg.inv(f["cell"]).T
+    nb = f["n_bloch"]
+    return lambda E, k: U.find_k_pc(E, k, reci_uc, rec_pc, dyn, int(max(nb[0], nb[1])))

@@ -1,7 +1,8 @@
 """GPU per-mode outputs (pf_transport_tdb_modes_permode_dev) turned into
 the reference's per-k mode files (write_specular / write_md,
-negf/write_data.f90:3-176) and checked against the reference's files of
-three k points."""
+negf/write_data.f90:3-176) -- with the primitive-cell columns of
+unfold_pc -- and checked against the reference's files of three k
+points, every column."""
 import os
 
 import numpy as np
@@ -9,7 +10,7 @@ import pytest
 
 from phinfortran_gb300.modes import LeadGeometry, mode_rows, transport_tdb_modes
 from phinfortran_gb300.output import write_mode_files
-from tests.sisi_case import sisi_blocks, sisi_params
+from tests.sisi_case import sisi_blocks, sisi_params, sisi_primitive_cell
 from tests.test_mode_files_host import FILES, compare_rows
 
 pytestmark = pytest.mark.gpu
@@ -33,7 +34,7 @@ def test_mode_files_against_reference(cuda_ready, sisi, tmp_path):
     cell = f["cell"]
     r = transport_tdb_modes(E, stacked, geo, f["kgrid"][ks], qidx=q, zero_flag=zf, lambda_eta=5e-3,
                             a_z_l=cell[2, 2], a_z_r=cell[2, 2], per_mode=True, **sisi_params(f))
-    rows = mode_rows(r, geo, f["kgrid"][ks], E, qidx=q)
+    rows = mode_rows(r, geo, f["kgrid"][ks], E, qidx=q, pc=sisi_primitive_cell(f))
     # the per-mode rows add up to the eight sums of the same run
     for name, key, col in (("trl", "transr_s", 11), ("tlr", "transl_s", 11), ("left", "refll_s", 11),
                            ("right", "reflr_s", 11)):

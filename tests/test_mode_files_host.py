@@ -9,7 +9,10 @@ import numpy as np
 import pytest
 
 from oracle import modes as M
+from oracle import unfold_pc as U
 from phinfortran_gb300.output import mode_file_line, write_mode_files
+from phinfortran_gb300.unfold_pc import read_primitive_cell_fdf
+from tests.sisi_case import sisi_find_pc, sisi_primitive_cell
 from tests.test_modes_host import oracle_point_sums
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -21,14 +24,14 @@ def perk():
     return np.load(os.path.join(HERE, "golden", "sisi_perk.npz"))
 
 
-def compare_rows(A, B, md):
+def compare_rows(A, B, md, pc=True):
     """Rows of one file against the reference's: the same energies, per
     energy the same number of rows and (after sorting by k, since the
     mode order inside an energy follows the eigen-solver) the same k within
     2e-9 (10-digit output), the sums within 5e-7 relative + 1e-12, the
     ratio r_s/r_t within 1e-9 where r_t > 1e-8 (below that it is the ratio
-    of two rounding-level reflections).  Columns 6-11 (primitive-cell k and
-    velocity) are not compared."""
+    of two rounding-level reflections); with ``pc`` the primitive-cell k
+    within 1e-8 and velocity within 1e-6 relative + 1e-9."""
     A, B = np.asarray(A, dtype=np.float64), np.asarray(B, dtype=np.float64)
 
     def groups(a):
@@ -50,6 +53,9 @@ def compare_rows(A, B, md):
         if not md:
             m = b[:, 12] > 1e-8
             assert (np.abs(a[m, 13] - b[m, 13]) <= 1e-9).all(), e
+        if pc:
+            assert np.abs(a[:, 5:8] - b[:, 5:8]).max() <= 1e-8, e
+            assert (np.abs(a[:, 8:11] - b[:, 8:11]) <= 1e-6 * np.abs(b[:, 8:11]) + 1e-9).all(), e
 
 
 def test_mode_file_line_matches_reference_text(perk):
@@ -73,11 +79,61 @@ def test_oracle_mode_rows_match_reference(sisi, perk, ik):
     geom = dict(ksc=f["kgrid"][ik], recivec=2 * np.pi * np.linalg.inv(f["cell_all"]).T, reci_uc_l=reci_uc,
                 reci_uc_r=reci_uc, nb=nb)
     rows = {n: [] for n in FILES}
+    find_pc = sisi_find_pc(f)
     for ie, (o, _) in enumerate(oracle_point_sums(f, ik, list(range(f["E"].size)))):
-        for n, rr in M.mode_file_rows(f["E"][ie], o, geom).items():
+        for n, rr in M.mode_file_rows(f["E"][ie], o, geom, find_pc).items():
             rows[n] += rr
     for n in FILES:
         compare_rows(rows[n], perk[f"{n}_{ik}"], n.startswith("md"))
+
+
+def test_primitive_cell_columns_match_reference(sisi, perk):
+    """find_k_pc from the k and energy of every row of the reference's
+    files (three k points, six files): the package's batched
+    PrimitiveCell.unfold for all rows, the oracle's loop restatement for
+    those of one file; both against the reference's k_pc and v_pc."""
+    pc = sisi_primitive_cell(sisi)
+    find_pc = sisi_find_pc(sisi)
+    nonzero = 0
+    for key in perk.files:
+        if key == "k_index":
+            continue
+        r = perk[key]
+        kp, vp = pc.unfold(r[:, 1] ** 2, r[:, 2:5])
+        assert np.abs(kp - r[:, 5:8]).max() <= 1e-8, key
+        assert (np.abs(vp - r[:, 8:11]) <= 1e-6 * np.abs(r[:, 8:11]) + 1e-9).all(), key
+        nonzero += int((np.abs(r[:, 5:11]) > 0).any(axis=1).sum())
+        if key == "mdr_37":
+            for row in r:
+                k1, v1 = find_pc(row[1] ** 2, row[2:5])
+                assert np.abs(k1 - row[5:8]).max() <= 1e-8
+                assert (np.abs(v1 - row[8:11]) <= 1e-6 * np.abs(row[8:11]) + 1e-9).all()
+    assert nonzero > 400          # the candidates search is exercised, not only the empty case
+
+
+def test_oracle_zone_flags_agree(sisi):
+    """in_ws of the oracle and zone_flags of the package on random and
+    boundary points of the primitive zone."""
+    from phinfortran_gb300.unfold_pc import zone_flags
+    rec = sisi_primitive_cell(sisi).recivec
+    rng = np.random.default_rng(3)
+    ks = np.concatenate([rng.uniform(-2, 2, (200, 3)), 0.5 * rec, 0.5 * (rec[0] + rec[1])[None]])
+    assert (zone_flags(rec, ks) == np.array([U.in_ws(rec, k) for k in ks])).all()
+    assert (zone_flags(rec, 0.5 * rec) == 2).all()
+
+
+def test_read_primitive_cell_fdf(tmp_path, sisi):
+    f = sisi
+    text = ["NumberOfAtoms 4", "NumberOfSpecies 1", f"LatticeConstant {float(f['pc_lscale'])} Ang",
+            "%block LatticeVectors"] + [" ".join(repr(float(x)) for x in v) for v in f["pc_latvec"]] + \
+           ["%endblock LatticeVectors", "%block AtomicScaledCoordinatesAndAtomicSpecies"] + \
+           [" ".join(repr(float(x)) for x in p) + f" {int(s)}" for p, s in zip(f["pc_scaled"], f["pc_species"])] + \
+           ["%endblock AtomicScaledCoordinatesAndAtomicSpecies"]
+    path = tmp_path / "pc.fdf"
+    path.write_text("\n".join(text) + "\n")
+    d = read_primitive_cell_fdf(str(path))
+    assert np.array_equal(d["latvec"], f["pc_latvec"]) and np.array_equal(d["scaled"], f["pc_scaled"])
+    assert np.array_equal(d["species"], f["pc_species"]) and d["lscale"] == float(f["pc_lscale"])
 
 
 def test_write_mode_files_appends_in_order(tmp_path, perk):
@@ -132,10 +188,11 @@ def test_mode_rows_assembly_matches_oracle_rows(sisi):
                     for lab in range(1, ns + 1):
                         res["col_sums"][a, mi, c, lab - 1] = M2[br == lab, c].sum()
     E = f["E"][ies]
-    got = mode_rows(res, geo, f["kgrid"][[ik]], E)
+    got = mode_rows(res, geo, f["kgrid"][[ik]], E, pc=sisi_primitive_cell(f))
+    find_pc = sisi_find_pc(f)
     for a, (o, _) in enumerate(pts):
-        want = M.mode_file_rows(E[a], o, geom)
+        want = M.mode_file_rows(E[a], o, geom, find_pc)
         for name in FILES:
             g = np.array(got[name][a][1], dtype=np.float64).reshape(-1, 15 if name.startswith("md") else 14)
             w = np.array(want[name], dtype=np.float64).reshape(g.shape)
-            np.testing.assert_allclose(g, w, rtol=1e-12, atol=1e-300, err_msg=f"{name} point {a}")
+            np.testing.assert_allclose(g, w, rtol=1e-9, atol=1e-12, err_msg=f"{name} point {a}")
