@@ -60,3 +60,22 @@ def test_argument_validation_of_later_entries_without_gpu(built_lib):
     rc = lib.pf_buttiker_tdb(64, 4, 4, 3, 1, *([None] * 8), 1, None, None, None, *([None] * 6),
                              0.0, 0.0, 10.0, 1e-14, 10, *([None] * 7), None)
     assert rc == -3
+
+
+def test_argument_validation_of_mode_entries_without_gpu(built_lib):
+    """The per-mode entry wants its three per-mode outputs together, and both
+    mode entries reject bad sizes on the host."""
+    import ctypes as C
+
+    from phinfortran_gb300 import _abi
+    lib = _abi.load()
+    kz = C.c_void_p(8)   # never dereferenced: the call is refused before any device work
+    args = (4, 4, 4, 2, 1, *([None] * 8), 1, None, None, None, 0.0, 1e-6, 10.0, 1e-14, 10, 5e-3, 1.0, 1.0, 1,
+            4, 4, None, 4, 4, None, None, None, None, None, None)
+    rc = lib.pf_transport_tdb_modes_permode_dev(*args, kz, None, None, None, 0, None)
+    assert rc == -1 and b"all given or all null" in lib.pf_modes_last_error()
+    bad = (0,) + args[1:]
+    rc = lib.pf_transport_tdb_modes_permode_dev(*bad, None, None, None, None, 0, None)
+    assert rc == -1 and b"positive" in lib.pf_modes_last_error()
+    rc = lib.pf_transport_tdb_modes_dev(*bad, None, 0, None)
+    assert rc == -1 and b"positive" in lib.pf_modes_last_error()
