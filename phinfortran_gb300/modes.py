@@ -243,6 +243,20 @@ def mode_rows(res, geometry, ksc, E, qidx=None, pc=None):
     labk = [geometry.label_k(k) for k in ksc]
     out = {name: [] for name in MODE_FILES}
     pcs = (pc, pc) if pc is None or not isinstance(pc, (tuple, list)) else tuple(pc)
+    # primitive-cell columns of the incoming modes of every point, one batch per side
+    pcol = {}
+    for kind, side in (("adv_l", 0), ("adv_r", 1)):
+        ki = KINDS.index(kind)
+        cols = np.zeros((npts, size[kind], 6))
+        if pcs[side] is not None:
+            kz, bz = res["mode_kz"][:, ki, :size[kind]], res["mode_bz"][:, ki, :size[kind]]
+            pp, ii = np.nonzero((kz < 99.9) & (bz > 0))
+            if pp.size:
+                lk = np.array([labk[int(q_of[a])][bz[a, i] - 1] for a, i in zip(pp, ii)])
+                lk[:, 2] = kz[pp, ii]
+                kp, vp = pcs[side].unfold(E[pp], lk)
+                cols[pp, ii, :3], cols[pp, ii, 3:] = kp, vp
+        pcol[kind] = cols
     for p in range(npts):
         q = int(q_of[p])
         lk = labk[q]
@@ -265,16 +279,7 @@ def mode_rows(res, geometry, ksc, E, qidx=None, pc=None):
             spec = float(np.sum(S[np.einsum("ij,ij->i", d, d) < 1.0e-5]))
             return _clamp(spec), _clamp(tot)
 
-        # incoming modes of each side with their primitive-cell columns
-        inc = {}
-        for kind, side in (("adv_l", 0), ("adv_r", 1)):
-            kb = kvec(kind)
-            pcols = np.zeros((size[kind], 6))
-            prop = np.nonzero(kb[:, 2] < 99.9)[0]
-            if pcs[side] is not None and prop.size:
-                kp, vp = pcs[side].unfold(E[p], kb[prop])
-                pcols[prop, :3], pcols[prop, 3:] = kp, vp
-            inc[kind] = (kb, pcols)
+        inc = {kind: (kvec(kind), pcol[kind][p]) for kind in ("adv_l", "adv_r")}
         for name, (mat, kind) in SPECULAR_FILES.items():
             kb, pcols = inc[kind]
             rows, c = [], 0

@@ -27,20 +27,24 @@ _LAT125 = np.array([(i1, i2, i3) for i1 in range(-2, 3) for i2 in range(-2, 3) f
                    dtype=np.float64)
 
 
-def zone_flags(a, ks):
+def zone_flags(a, ks, chunk=4096):
     """Per row of ks: 2 when the two nearest points of the lattice a (rows)
     are equally near within 1e-5 (zone boundary), 1 when the origin is the
     nearest, 0 otherwise (negf/util.f90:589-638, 125 lattice points)."""
     ks = np.atleast_2d(np.asarray(ks, dtype=np.float64))
-    d = ks[:, None, :] - (_LAT125 @ a)[None]
-    dist = np.einsum("kij,kij->ki", d, d)
-    first = np.argmin(dist, axis=1)
-    rows = np.arange(ks.shape[0])
-    dmin = dist[rows, first]
-    dist2 = dist.copy()
-    dist2[rows, first] = np.inf
-    flag = np.where(np.abs(dist[:, 62] - dmin) < 1.0e-5, 1, 0)
-    return np.where(np.abs(dist2.min(axis=1) - dmin) < 1.0e-5, 2, flag)
+    lat = _LAT125 @ a
+    out = np.zeros(ks.shape[0], dtype=np.int64)
+    for s0 in range(0, ks.shape[0], chunk):
+        part = ks[s0:s0 + chunk]
+        d = part[:, None, :] - lat[None]
+        dist = np.einsum("kij,kij->ki", d, d)
+        first = np.argmin(dist, axis=1)
+        rows = np.arange(part.shape[0])
+        dmin = dist[rows, first]
+        flag = np.where(np.abs(dist[:, 62] - dmin) < 1.0e-5, 1, 0)   # index 62: the origin
+        dist[rows, first] = np.inf                                    # second smallest next
+        out[s0:s0 + chunk] = np.where(np.abs(dist.min(axis=1) - dmin) < 1.0e-5, 2, flag)
+    return out
 
 
 class PrimitiveCell:
@@ -68,6 +72,7 @@ class PrimitiveCell:
         self.l = int(l)
         mass = np.asarray(mass_no, dtype=np.float64)[np.asarray(species) - 1]
         self._terms(qe, mass)
+        self.zone_radius2 = (0.5 * np.linalg.norm(self.recivec, axis=1).sum() + 1.0e-3) ** 2
         g = np.arange(-self.l, self.l + 1, dtype=np.float64)
         self.gshift = np.stack(np.meshgrid(g, g, g, indexing="ij"), axis=-1).reshape(-1, 3) @ self.reci_uc
 
@@ -95,71 +100,93 @@ class PrimitiveCell:
                     blk = fc[:, :, i, j, ia % nx, ib % ny, ic % nz] / nreq[t] / np.sqrt(mass[i] * mass[j])
                     blocks[i][j % na].append(blk)
                     bonds[i][j % na].append(dr[t])
-        self.blocks = [[np.array(b) for b in row] for row in blocks]
-        self.bonds = [[np.array(b) for b in row] for row in bonds]
+        # all terms stacked: the phases of a batch of k are one exp, each
+        # (i, j) block one (B x T_ij) x (T_ij x 9) product
+        self.bonds = np.concatenate([np.array(bonds[i][j]).reshape(-1, 3) for i in range(na) for j in range(na)])
+        self.spans, t = [], 0
+        for i in range(na):
+            for j in range(na):
+                nt = len(blocks[i][j])
+                self.spans.append((i, j, t, t + nt, np.array(blocks[i][j]).reshape(nt, 9).astype(np.complex128)))
+                t += nt
 
     def dynamical(self, ks):
         """(B, 3 na, 3 na) Hermitised dynamical matrices at the rows of ks."""
         ks = np.atleast_2d(np.asarray(ks, dtype=np.float64))
+        return self._from_phases(np.exp(1j * (ks @ self.bonds.T)))
+
+    def _from_phases(self, ph):
         na = self.natoms
-        out = np.zeros((ks.shape[0], 3 * na, 3 * na), dtype=np.complex128)
-        for i in range(na):
-            for j in range(na):
-                ph = np.exp(1j * (ks @ self.bonds[i][j].T))
-                out[:, 3 * i:3 * i + 3, 3 * j:3 * j + 3] = np.einsum("bt,tmn->bmn", ph, self.blocks[i][j])
+        out = np.zeros((ph.shape[0], 3 * na, 3 * na), dtype=np.complex128)
+        for i, j, t0, t1, blk in self.spans:
+            out[:, 3 * i:3 * i + 3, 3 * j:3 * j + 3] = (ph[:, t0:t1] @ blk).reshape(-1, 3, 3)
         return 0.5 * (out + np.conj(np.swapaxes(out, 1, 2)))
 
     def bands(self, ks, step=1.0e-5):
         """Eigenvalues (ascending) and band velocities (central differences
         of D with step 1e-5) at the rows of ks."""
         ks = np.atleast_2d(np.asarray(ks, dtype=np.float64))
-        eigs, evs = np.linalg.eigh(self.dynamical(ks))
+        ph = np.exp(1j * (ks @ self.bonds.T))
+        eigs, evs = np.linalg.eigh(self._from_phases(ph))
         vel = np.zeros(eigs.shape + (3,))
         for d in range(3):
-            e = np.zeros(3)
-            e[d] = step
-            dh = (self.dynamical(ks + e) - self.dynamical(ks - e)) / (2.0 * step)
+            # exp(i (k +- step e_d).r) = exp(i k.r) exp(+- i step r_d)
+            shift = np.exp(1j * step * self.bonds[:, d])
+            dh = (self._from_phases(ph * shift) - self._from_phases(ph * np.conj(shift))) / (2.0 * step)
             proj = np.einsum("bim,bij,bjm->bm", np.conj(evs), dh, evs)
             vel[:, :, d] = np.real(proj) / (2 * np.sqrt(np.abs(eigs)))
         return eigs, vel
 
     def unfold(self, E, ks):
         """(k_pc, v_pc) for modes with unfolded wavevectors ks (rows) at the
-        energies E (omega^2), zeros where no candidate matches."""
+        energies E (omega^2), zeros where no candidate matches.  All
+        candidates of all modes are solved in one batch."""
         ks = np.atleast_2d(np.asarray(ks, dtype=np.float64))
-        E = np.broadcast_to(np.asarray(E, dtype=np.float64), (ks.shape[0],))
-        edge = zone_flags(self.reci_uc, ks) == 2
-        owner, cand = [], []
-        for m in range(ks.shape[0]):
-            if edge[m]:
-                c = ks[m][None]
-            else:
-                c = ks[m][None] + self.gshift
-                c = c[zone_flags(self.recivec, c) != 0]
-            owner.extend([m] * c.shape[0])
-            cand.append(c)
+        nm = ks.shape[0]
+        E = np.broadcast_to(np.asarray(E, dtype=np.float64), (nm,))
         kpc = np.zeros_like(ks)
         vpc = np.zeros_like(ks)
-        if not owner:
+        if nm == 0:
             return kpc, vpc
-        owner = np.array(owner)
-        cand = np.concatenate(cand)
+        edge = zone_flags(self.reci_uc, ks) == 2
+        allc = ks[:, None, :] + self.gshift[None]
+        # a point of the primitive zone (boundary included) is within half the
+        # summed lengths of the reciprocal vectors: only those are tested
+        flat = allc.reshape(-1, 3)
+        near = np.einsum("ij,ij->i", flat, flat) <= self.zone_radius2
+        inside = np.zeros(flat.shape[0], dtype=bool)
+        inside[near] = zone_flags(self.recivec, flat[near]) != 0
+        inside = inside.reshape(nm, -1)
+        inside[edge] = False
+        own_n, g_n = np.nonzero(inside)               # grouped by mode, candidates in search order
+        own_e = np.nonzero(edge)[0]
+        owner = np.concatenate([own_e, own_n])
+        cand = np.concatenate([ks[own_e], allc[own_n, g_n]])
+        if owner.size == 0:
+            return kpc, vpc
         eigs, vel = self.bands(cand)
         hit = np.abs(np.sqrt(E[owner])[:, None] - np.sqrt(np.abs(eigs))) < 1.0e-2
         any_hit = hit.any(axis=1)
-        last = eigs.shape[1] - 1 - np.argmax(hit[:, ::-1], axis=1)       # the last matching band
-        v_c = vel[np.arange(cand.shape[0]), last]
-        for m in range(ks.shape[0]):
-            idx = np.nonzero(owner == m)[0]
-            if edge[m]:
-                kpc[m] = ks[m]                                    # kept even without a band match
-                if any_hit[idx[0]]:
-                    vpc[m] = v_c[idx[0]]
-                continue
-            idx = idx[any_hit[idx]]
-            if idx.size:
-                kpc[m] = cand[idx[np.argmin(np.linalg.norm(cand[idx], axis=1))]]
-                vpc[m] = v_c[idx[0]]
+        last = eigs.shape[1] - 1 - np.argmax(hit[:, ::-1], axis=1)      # the last matching band
+        v_c = vel[np.arange(owner.size), last]
+        ne = own_e.size
+        # zone-boundary modes keep k; the velocity only when a band matches
+        kpc[own_e] = ks[own_e]
+        he = np.nonzero(any_hit[:ne])[0]
+        vpc[own_e[he]] = v_c[he]
+        # the others: among matching candidates the smallest |k| (first on
+        # ties) and the velocity of the first
+        idx = ne + np.nonzero(any_hit[ne:])[0]
+        if idx.size:
+            o = owner[idx]
+            _, first = np.unique(o, return_index=True)
+            vpc[o[first]] = v_c[idx[first]]
+            norm = np.linalg.norm(cand[idx], axis=1)
+            order = np.lexsort((np.arange(idx.size), norm, o))
+            o_sorted = o[order]
+            keep = np.ones(order.size, dtype=bool)
+            keep[1:] = o_sorted[1:] != o_sorted[:-1]
+            kpc[o_sorted[keep]] = cand[idx[order[keep]]]
         return kpc, vpc
 
 
