@@ -196,3 +196,36 @@ def test_mode_rows_assembly_matches_oracle_rows(sisi):
             g = np.array(got[name][a][1], dtype=np.float64).reshape(-1, 15 if name.startswith("md") else 14)
             w = np.array(want[name], dtype=np.float64).reshape(g.shape)
             np.testing.assert_allclose(g, w, rtol=1e-9, atol=1e-12, err_msg=f"{name} point {a}")
+
+
+def test_mode_rows_from_oracle_modes_match_reference_files(sisi, perk):
+    """The whole host half of the per-k files -- mode_rows on the per-mode
+    data the GPU entry returns (here built from the oracle's matrices) with
+    the package's primitive-cell unfolding -- against the reference's six
+    files of k = 1, every energy and every column."""
+    from phinfortran_gb300.modes import KINDS, MATRICES, LeadGeometry, mode_rows
+
+    f, ik = sisi, 0
+    nb = tuple(int(x) for x in f["n_bloch"])
+    b, p = int(f["buffer"]), int(f["period"])
+    geo = LeadGeometry.from_qe(f["pos_all"], f["cell"], f["cell_all"], nb, b, p, b, p)
+    pts = oracle_point_sums(f, ik, list(range(f["E"].size)))
+    nl, nr = pts[0][0]["rll"].shape[0], pts[0][0]["rrr"].shape[0]
+    mm, ns = max(nl, nr), nb[0] * nb[1]
+    res = dict(mode_kz=np.zeros((len(pts), 4, mm)), mode_bz=np.zeros((len(pts), 4, mm), np.int32),
+               col_sums=np.zeros((len(pts), 4, mm, ns)), nl=nl, nr=nr)
+    rows_of = {"tlr": ("ret_l", "adv_r"), "trl": ("ret_r", "adv_l"), "rrr": ("ret_r", "adv_r"),
+               "rll": ("ret_l", "adv_l")}
+    for a, (o, _) in enumerate(pts):
+        md = o["modes"]
+        for ki, kind in enumerate(KINDS):
+            res["mode_kz"][a, ki, :md[kind]["kz"].size] = md[kind]["kz"]
+            res["mode_bz"][a, ki, :md[kind]["bz"].size] = md[kind]["bz"]
+        for mi, mat in enumerate(MATRICES):
+            m2 = np.abs(o[mat]) ** 2
+            br, bc = md[rows_of[mat][0]]["bz"], md[rows_of[mat][1]]["bz"]
+            for c in np.nonzero(bc > 0)[0]:
+                res["col_sums"][a, mi, c] = [m2[br == lab, c].sum() for lab in range(1, ns + 1)]
+    rows = mode_rows(res, geo, f["kgrid"][[ik]], f["E"], pc=sisi_primitive_cell(f))
+    for name in FILES:
+        compare_rows([r for _, rr in rows[name] for r in rr], perk[f"{name}_{ik}"], name.startswith("md"))
