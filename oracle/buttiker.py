@@ -24,7 +24,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .negf import H, decimate, lead_eps, surface_green_tdb
+from .negf import H, lead_eps, surface_green_tdb
 
 PI = 3.141592653589793238     # negf/util.f90:5
 KB = 1.380649e-23             # negf/util.f90:9

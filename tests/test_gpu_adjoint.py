@@ -4,7 +4,6 @@ import numpy as np
 import pytest
 
 from oracle import adjoint as A
-from oracle import negf as N
 from phinfortran_gb300 import systems as S
 from phinfortran_gb300 import transport_tdb
 from phinfortran_gb300.gradients import conductance_fn, landauer_weights, transport_grad

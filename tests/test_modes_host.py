@@ -2,7 +2,6 @@
 vel_mat_tdb against the reference's golden si-si sums, and the package's
 unfolding geometry against the oracle's."""
 import numpy as np
-import pytest
 
 from oracle import modes as M
 from oracle import negf as N
