@@ -126,28 +126,44 @@ def measure_peak(torch, dtype, n):
 
 
 def cpu_oracle_rate(E, blocks, p, budget_s=12.0, min_pts=16):
-    """Oracle solves/s on the host cores for a bounded sample of the workload."""
-    from oracle import negf as N
+    """Oracle solves/s on the host cores for a bounded sample of the workload:
+    the C restatement of the FP64 oracle (oracle/negf_c.c, every host
+    thread, one energy per OpenMP iteration); the numpy oracle if the C
+    one cannot be built."""
     try:
-        from threadpoolctl import threadpool_info
-        cores = max([i.get("num_threads", 1) for i in threadpool_info()] or [1])
-    except Exception:  # noqa: BLE001
-        cores = os.cpu_count() or 1
+        from oracle.negf_c import transport_c
+        threads = os.cpu_count() or 1
+
+        def solve(Es):
+            return transport_c(Es, blocks, p["eta"], p["eta0"], p["convergence"], p["dev_factor"],
+                               threads=threads)[2]
+        what = "C restatement of the FP64 oracle, OpenMP over energies"
+        cores = solve(E[:1])
+    except (OSError, ImportError, subprocess.CalledProcessError):
+        from oracle import negf as N
+        try:
+            from threadpoolctl import threadpool_info
+            cores = max([i.get("num_threads", 1) for i in threadpool_info()] or [1])
+        except Exception:  # noqa: BLE001
+            cores = os.cpu_count() or 1
+
+        def solve(Es):
+            N.transport(Es, blocks, p["eta"], p["eta0"], p["convergence"], p["dev_factor"], want_plus_minus=False)
+        what = "numpy FP64 oracle"
     npts = min_pts
     idx = np.linspace(0, len(E) - 1, npts).astype(int)
     t0 = time.perf_counter()
-    N.transport(E[idx], blocks, p["eta"], p["eta0"], p["convergence"], p["dev_factor"], want_plus_minus=False)
+    solve(E[idx])
     dt = time.perf_counter() - t0
     # grow the sample to roughly `budget_s` of CPU work
     if dt < budget_s / 2:
         npts2 = int(min(len(E), max(npts, npts * budget_s / max(dt, 1e-3))))
         idx = np.linspace(0, len(E) - 1, npts2).astype(int)
         t0 = time.perf_counter()
-        N.transport(E[idx], blocks, p["eta"], p["eta0"], p["convergence"], p["dev_factor"],
-                    want_plus_minus=False)
+        solve(E[idx])
         dt = time.perf_counter() - t0
         npts = npts2
-    return npts / dt, cores, f"{npts} of {len(E)} energies (uniform stride), T_L only, numpy FP64 oracle"
+    return npts / dt, cores, f"{npts} of {len(E)} energies (uniform stride), T_L only, {what}"
 
 
 def build_workload():
