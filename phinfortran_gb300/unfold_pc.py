@@ -51,8 +51,8 @@ class PrimitiveCell:
     """Primitive cell of a lead: the QE force constants folded onto its
     atoms, its reciprocal vectors and the unit cell's.
 
-    qe: dict(pos, cell, fc (3,3,nat,nat,nx,ny,nz), rws, rd, nxyz) of the QE
-    force-constant file as read_qe_fc processes it; latvec (3x3 rows) and
+    qe: dict(pos, cell, fc (3,3,nat,nat,nx,ny,nz), rws, rd and nxyz or
+    nx/ny/nz) of the QE force-constant file, as qe_input.read_qe_fc gives it; latvec (3x3 rows) and
     scaled (natoms_uc, 3) with species (1-based) and the lattice constant of
     the primitive-cell input (pc1.fdf style; the vectors are turned by
     pi/4 about z as negf/input.f90:617 does); mass_no: species masses;
@@ -78,7 +78,7 @@ class PrimitiveCell:
 
     def _terms(self, qe, mass):
         pos, cell, fc, rws, rd = qe["pos"], qe["cell"], qe["fc"], qe["rws"], qe["rd"]
-        nx, ny, nz = (int(x) for x in qe["nxyz"])
+        nx, ny, nz = (int(x) for x in (qe["nxyz"] if "nxyz" in qe else (qe["nx"], qe["ny"], qe["nz"])))
         n = np.arange
         abc = np.stack(np.meshgrid(n(-2 * nx, 2 * nx + 1), n(-2 * ny, 2 * ny + 1), n(-2 * nz, 2 * nz + 1),
                                    indexing="ij"), axis=-1).reshape(-1, 3).astype(np.float64)

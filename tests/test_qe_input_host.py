@@ -70,3 +70,18 @@ def test_reader_reproduces_fixture_from_reference_files(sisi):
     assert np.array_equal(P.read_species_masses(os.path.join(REF, "trans_input.fdf")), sisi["mass_no"])
     prof = P.read_mass_profile(os.path.join(REF, "mass_profile.dat"))
     assert np.array_equal(sisi["mass_no"][prof - 1], sisi["mass_all"])
+
+
+def test_primitive_cell_takes_the_reader_dict(sisi):
+    """unfold_pc.PrimitiveCell accepts read_qe_fc's dict (nx, ny, nz keys)
+    as well as the fixture's nxyz."""
+    from phinfortran_gb300.unfold_pc import PrimitiveCell
+    from tests.sisi_case import sisi_primitive_cell
+    f = sisi
+    qe = dict(pos=f["pos"], cell=f["cell"], fc=f["fc"], rws=f["rws"], rd=f["rd"], nx=int(f["nxyz"][0]),
+              ny=int(f["nxyz"][1]), nz=int(f["nxyz"][2]))
+    a = PrimitiveCell(qe, f["pc_latvec"], f["pc_scaled"], f["pc_species"], float(f["pc_lscale"]), f["mass_no"],
+                      2 * np.pi * np.linalg.inv(f["cell"]).T, 2)
+    b = sisi_primitive_cell(f)
+    k = np.array([[0.3, -0.2, 0.4], [0.0, 0.0, 0.1]])
+    assert np.array_equal(a.dynamical(k), b.dynamical(k))
