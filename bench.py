@@ -137,7 +137,7 @@ def cpu_oracle_rate(E, blocks, p, budget_s=12.0, min_pts=16):
         def solve(Es):
             return transport_c(Es, blocks, p["eta"], p["eta0"], p["convergence"], p["dev_factor"],
                                threads=threads)[2]
-        what = "C restatement of the FP64 oracle, OpenMP over energies"
+        what = "C restatement of the FP64 oracle (oracle/negf_c.c), OpenMP over energies"
         cores = solve(E[:1])
     except (OSError, ImportError, subprocess.CalledProcessError):
         from oracle import negf as N
@@ -149,7 +149,7 @@ def cpu_oracle_rate(E, blocks, p, budget_s=12.0, min_pts=16):
 
         def solve(Es):
             N.transport(Es, blocks, p["eta"], p["eta0"], p["convergence"], p["dev_factor"], want_plus_minus=False)
-        what = "numpy FP64 oracle"
+        what = "numpy restatement of the FP64 oracle (oracle/negf.py)"
     npts = min_pts
     idx = np.linspace(0, len(E) - 1, npts).astype(int)
     t0 = time.perf_counter()
@@ -163,7 +163,7 @@ def cpu_oracle_rate(E, blocks, p, budget_s=12.0, min_pts=16):
         solve(E[idx])
         dt = time.perf_counter() - t0
         npts = npts2
-    return npts / dt, cores, f"{npts} of {len(E)} energies (uniform stride), T_L only, {what}"
+    return npts / dt, cores, f"{npts} of {len(E)} energies (uniform stride), T_L only, {what}", what
 
 
 def build_workload():
@@ -182,8 +182,8 @@ def run_reference(args):
     vals = []
     info = None
     for i in range(args.warmup + args.steps):
-        v, cores, sample = cpu_oracle_rate(E, b, p, budget_s=args.ref_budget)
-        info = (cores, sample)
+        v, cores, sample, what = cpu_oracle_rate(E, b, p, budget_s=args.ref_budget)
+        info = (cores, sample, what)
         if i >= args.warmup:
             vals.append(v)
     v = statistics.median(vals)
@@ -195,7 +195,7 @@ def run_reference(args):
                 cpu_baseline=dict(value=v, unit="solves/s", cores=info[0], kind="port", sample=info[1]),
                 e2e=dict(value=v, unit="solves/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0),
                 note="reference Fortran/MPI/MKL build is not compilable here (no Fortran, MPI or LAPACK); "
-                     "the timed CPU implementation is the FP64 numpy restatement of the path")
+                     f"the timed CPU implementation is the {info[2]} of the path")
     print(json.dumps(line), flush=True)
 
 
@@ -451,7 +451,7 @@ def main():
 
     cpu = None
     if not args.no_cpu_baseline:
-        v, cores, sample = cpu_oracle_rate(E, b, p)
+        v, cores, sample, _ = cpu_oracle_rate(E, b, p)
         cpu = dict(value=v, unit="solves/s", cores=cores, kind="port", sample=sample)
 
     if args.path == "fp64":

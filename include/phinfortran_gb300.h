@@ -4,7 +4,7 @@
  * Drop-in for the per-(ie,ik) hot loop of KitchenSong/phinfortran's tdb
  * transport branch (negf/phinfortran.f90:1188-1251).  The Fortran driver
  * keeps its input readers, grids and output writers and calls these
- * functions through iso_c_binding (see INTEGRATION.md).
+ * functions through iso_c_binding.
  *
  * Conventions (those of the reference's arrays):
  *  - every matrix is complex(kind=8), column-major, passed as double* to
@@ -127,7 +127,7 @@ int pf_transport_tdb(int n, int nl, int nr, int L, int nq,
  *     lead+device matrix), and the last block column G_{:,N+1} is refined
  *     against a double-float residual: one sweep for every point, then up
  *     to refine_iters - 1 more for each point whose last correction of the
- *     block X_0 = G_{0,N+1} was above 1e-5 relative to X_0 (refine_iters
+ *     block X_0 = G_{0,N+1} was above 3e-5 (PF_REFINE_TOL) relative to X_0 (refine_iters
  *     in [0, 16]; 0 keeps the FP32 solution);
  *   - the Caroli trace (negf/lesser.f90:787-792) is taken in double-float.
  * The per-point matrix work uses no FP64 arithmetic.  work must hold
@@ -266,7 +266,9 @@ const char* pf_grad_last_error(void);
  * are rejected with PF_ERR_SIZE, and large batches run with fewer
  * concurrent CTAs.  The first call on a device resolves the array's device
  * address (cudaGetSymbolAddress, with that device current); make that first
- * call before any stream capture.  All calls share the array: calls whose
+ * call before any stream capture.  The address belongs to the device's
+ * CUDA context: after a device reset the next call resolves it again, so
+ * that call too must come before any capture.  All calls share the array: calls whose
  * kernels overlap on the GPU (concurrent streams, several host threads)
  * race on it and must be serialised by the caller.
  */
@@ -483,7 +485,7 @@ int pf_gen_dyn_dev(int natoms, int fc_rows, const double* force_constant,
                    const int* pair_off, const int* ent_idx,
                    const double* ent_dr, const int* row_atom,
                    const double* mass, int nq, const double* kcart,
-                   int hermitize, double* H, cudaStream_t stream);
+                   int hermitize, double* H, void* stream);
 
 /* Block set of the tdb transport entries taken from nq dense matrices
  * (column-major norb x norb complex, device) as the full-Hamiltonian path
@@ -501,7 +503,7 @@ int pf_dense_to_tdb_dev(int norb, int nq, const double* H, int nl, int nr,
                         const int* layer_start, int n, double* HL,
                         double* HLv, double* HR, double* HRv, double* Hd,
                         double* Hdv, double* Hld, double* Hrd, int* bad,
-                        cudaStream_t stream);
+                        void* stream);
 
 /* Message for the last error of the full-Hamiltonian entries. */
 const char* pf_fullh_last_error(void);

@@ -204,7 +204,8 @@ const char* pf_fullh_last_error(void) { return g_err; }
 
 int pf_gen_dyn_dev(int natoms, int fc_rows, const double* fc, int npairs, const int* pair_a, const int* pair_b,
                    const int* pair_off, const int* ent_idx, const double* ent_dr, const int* row_atom,
-                   const double* mass, int nq, const double* kcart, int hermitize, double* H, cudaStream_t stream) {
+                   const double* mass, int nq, const double* kcart, int hermitize, double* H, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
   if (natoms <= 0 || fc_rows <= 0 || npairs < 0 || nq <= 0) return set_err(PF_ERR_ARG, "pf_gen_dyn: bad sizes");
   if (!fc || !row_atom || !mass || !kcart || !H || (npairs > 0 && (!pair_a || !pair_b || !pair_off || !ent_idx ||
                                                                     !ent_dr)))
@@ -291,7 +292,8 @@ int pf_gen_dyn(int natoms, int nbx, int nby, int n_uc, int nz, int fc_rows, int 
 
 int pf_dense_to_tdb_dev(int norb, int nq, const double* H, int nl, int nr, int n_buffer_l, int n_buffer_r, int L,
                         const int* layer_start, int n, double* HL, double* HLv, double* HR, double* HRv, double* Hd,
-                        double* Hdv, double* Hld, double* Hrd, int* bad, cudaStream_t stream) {
+                        double* Hdv, double* Hld, double* Hrd, int* bad, void* stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
   if (norb <= 0 || nq <= 0 || nl <= 0 || nr <= 0 || n_buffer_l < 0 || n_buffer_r < 0 || L <= 0 || n <= 0)
     return set_err(PF_ERR_ARG, "pf_dense_to_tdb: bad sizes");
   if (n_buffer_l + 2 * nl + n_buffer_r + 2 * nr >= norb)

@@ -1048,23 +1048,74 @@ size_t mixed_workspace_bytes(int n, int nl, int nr, int L, int nq, int npts) {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[PF_NOALLOC_SCRATCH_BYTES];
 
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[128] = {};
+struct NoallocSlot {
+  void* ptr;
+  unsigned long long ctx_id;  // the CUDA context the address belongs to
+};
+NoallocSlot g_noalloc_slot[128] = {};
 
-// Device address of the static scratch for the current device; resolved
-// once per device (the first call on a device does it, with that device
-// current).
-int noalloc_scratch(void** out) {
+// Driver calls that identify the current context, fetched through the
+// runtime (the library does not link libcuda itself).
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+int current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2) {
+      (void)cudaGetLastError();
+      return set_err(PF_ERR_CUDA, "pf_transport_tdb_noalloc: driver context queries unavailable");
+    }
+    get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  void* ctx = nullptr;
+  *id = 0;
+  if (get_current(&ctx) != 0) return set_err(PF_ERR_CUDA, "pf_transport_tdb_noalloc: cuCtxGetCurrent failed");
+  if (ctx && get_id(ctx, id) != 0) return set_err(PF_ERR_CUDA, "pf_transport_tdb_noalloc: cuCtxGetId failed");
+  return PF_SUCCESS;
+}
+
+// Device address of the static scratch for the current device.  Set-up,
+// once per device: the first call on a device (with that device current)
+// resolves it with cudaGetSymbolAddress; later calls reuse it.  The address
+// is tied to the device's CUDA context: after a device reset the next call
+// runs in a new context (a new context id) and resolves the address again,
+// since the reloaded module may place the array elsewhere.  The set-up call
+// must not be captured into a CUDA graph (it may load the module): a call
+// that would need the set-up during stream capture is refused.
+int noalloc_scratch(cudaStream_t stream, void** out) {
   int dev = 0;
   PF_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 128) return set_err(PF_ERR_ARG, "pf: device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  unsigned long long id = 0;
+  int rc = current_context_id(&id);
+  if (rc != PF_SUCCESS) return rc;
+  NoallocSlot& slot = g_noalloc_slot[dev];
+  if (id == 0 || !slot.ptr || slot.ctx_id != id) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const cudaError_t qe = cudaStreamIsCapturing(stream, &cap);
+    if (qe != cudaSuccess) (void)cudaGetLastError();
+    if (qe != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+      return set_err(PF_ERR_ARG,
+                     "pf_transport_tdb_noalloc: first call on this device (or after a device reset) made "
+                     "during stream capture; make one call outside capture first");
     void* ptr = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_err(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-    g_noalloc_ptr[dev] = ptr;
+    rc = current_context_id(&id);  // the lookup creates the context when none was current
+    if (rc != PF_SUCCESS) return rc;
+    slot.ptr = ptr;
+    slot.ctx_id = id;
   }
-  *out = g_noalloc_ptr[dev];
+  *out = slot.ptr;
   return PF_SUCCESS;
 }
 
@@ -1088,7 +1139,7 @@ int launch_transport_noalloc(const pf::System<double>& sys, const pf::Points& pt
   const size_t cap = ((size_t)PF_NOALLOC_SCRATCH_BYTES - fixed) / lay.per_cta_bytes;
   if ((size_t)grid > cap) grid = (int)cap;
   void* base = nullptr;
-  int rc = noalloc_scratch(&base);
+  int rc = noalloc_scratch(stream, &base);
   if (rc != PF_SUCCESS) return rc;
   int* queue = reinterpret_cast<int*>(base);
   int* mirror = reinterpret_cast<int*>(reinterpret_cast<char*>(base) + 256);

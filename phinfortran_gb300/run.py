@@ -11,8 +11,8 @@ Modes: ``transport`` (T per point), ``modes`` (T plus the s/ns sums of the
 mode-resolved transmission; si-si fixture only), ``grad`` (adjoint: T and
 the block sensitivities of the Landauer conductance).  ``--perturb r``
 multiplies every block entry by (1 + r N(0,1)) first: two runs with and
-without it give the FP64 conditioning of each point.  Used for timing and
-for the ncu captures summarised under profiles/.
+without it give the FP64 conditioning of each point.  The summary gives
+the wall time, the mean decimation count, the status words and T.
 """
 from __future__ import annotations
 

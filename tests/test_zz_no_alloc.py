@@ -81,12 +81,24 @@ def test_noalloc_matches_workspace_entry(cuda_ready, case):
 
 
 def test_noalloc_rejects_oversized_problem(cuda_ready):
-    """A q count whose scratch exceeds the static maximum is refused cleanly."""
+    """A q count whose scratch exceeds the static maximum is refused cleanly.
+    Every pointer is a real device buffer holding the blocks of q = 0, the
+    one point uses q = 0 and the leads differ in size (so no lead-mirror
+    pass over all q is made): a refusal that came too late would still only
+    read valid memory."""
+    import torch
     lib = _abi.load()
-    n = 4
+    n, nl, nr = 4, 4, 6
     nq = (64 << 20) // 4          # lead-mirror flags alone exceed the 32 MiB array
-    rc = lib.pf_transport_tdb_noalloc(n, n, n, 1, nq, *([C.c_void_p(16)] * 8), 1, C.c_void_p(16), None, None,
-                                      0.0, 1e-6, 1.0, 1e-14, 10, 0, C.c_void_p(16), None, C.c_void_p(16), None,
-                                      None)
+    sizes = [nl * nl, nl * nl, nr * nr, nr * nr, n * n, 0, nl * n, nr * n]
+    blocks = [torch.zeros(2 * max(s, 1), dtype=torch.float64, device="cuda") for s in sizes]
+    E = torch.ones(1, dtype=torch.float64, device="cuda")
+    tl = torch.zeros(1, dtype=torch.float64, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    qidx = torch.zeros(1, dtype=torch.int32, device="cuda")
+    rc = lib.pf_transport_tdb_noalloc(n, nl, nr, 1, nq, *[b.data_ptr() for b in blocks], 1, E.data_ptr(),
+                                      qidx.data_ptr(), None, 0.0, 1e-6, 1.0, 1e-14, 10, 0, tl.data_ptr(), None,
+                                      st.data_ptr(), None, None)
+    torch.cuda.synchronize()
     assert rc == -3
     assert b"static maximum" in lib.pf_last_error()
