@@ -230,6 +230,9 @@ const char* pf_cond_last_error(void);
  */
 #define PF_ARITH_FP64 0
 #define PF_ARITH_DF64 1
+/* The FP64 algorithm with its block products on the tensor cores as exact
+ * BF16 slice products (see pf_tc_zgemm_dev); large-block entry only. */
+#define PF_ARITH_TC 2
 
 size_t pf_transport_tdb_grad_workspace_size(int n, int nl, int nr, int L,
                                             int nq, int npts, int ckpt,
@@ -384,9 +387,11 @@ const char* pf_modes_last_error(void);
  * grouped by q and advanced in batches through batched tile kernels (block
  * GEMMs, a blocked Gauss-Jordan inverse, masked decimation steps).  The call
  * is synchronous with respect to `stream` (the decimation loop reads one
- * counter per step).  arith: PF_ARITH_FP64, or PF_ARITH_DF64 (every block
+ * counter per step).  arith: PF_ARITH_FP64, PF_ARITH_DF64 (every block
  * operation in double-float pairs on the FP32 pipe, ~48 significant bits;
- * the q block set is converted once into the workspace).
+ * the q block set is converted once into the workspace) or PF_ARITH_TC (the
+ * FP64 algorithm with every block product on the tcgen05 tensor cores as
+ * exact BF16 slice products, FP64-grade; the inverse panels stay FP64).
  * work: pf_transport_tdb_tiled_workspace_size bytes.
  */
 #define PF_NMAX_TILED 2048
@@ -408,6 +413,34 @@ int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq,
 
 /* Message for the last error of the large-block entry points. */
 const char* pf_tiled_last_error(void);
+
+/*
+ * Batched FP64-grade complex GEMM on the tcgen05 tensor cores.  No
+ * counterpart in the reference (it is the block product the large-block
+ * transport path is built on, exported for drivers that keep their own
+ * recursion, e.g. negf/lesser.f90:587-589, 608 or negf/surface.f90:488-497):
+ *     C_b = alpha op(A_b) op(B_b) + beta C_b,   b = 0 .. batch-1,
+ * op = 'N' or 'C' (conjugate transpose), complex(kind=8) column-major
+ * device arrays, real alpha and beta, batch strides in complex elements
+ * (0 shares an operand).  Every row of op(A) and column of op(B) is scaled
+ * by a power of two and split into eight 7-bit BF16 slices; the slice
+ * products that matter are summed exactly on the tensor cores (FP32
+ * accumulation of integers below 2^22) and assembled in FP64, so the
+ * result has the accuracy of an FP64 GEMM (error O(k 2^-55) |A| |B|).
+ * work: pf_tc_zgemm_workspace_size bytes of device memory (a_shared /
+ * b_shared: strideA / strideB == 0).  Synchronous on `stream`.
+ */
+size_t pf_tc_zgemm_workspace_size(int m, int n, int k, int batch,
+                                  int a_shared, int b_shared);
+
+int pf_tc_zgemm_dev(int transa, int transb, int m, int n, int k,
+                    double alpha, const double* A, int lda, long long strideA,
+                    const double* B, int ldb, long long strideB, double beta,
+                    double* C, int ldc, long long strideC, int batch,
+                    void* work, size_t work_bytes, void* stream);
+
+/* Message for the last error of pf_tc_zgemm_dev. */
+const char* pf_tc_last_error(void);
 
 /*
  * Tight-binding H(k) blocks (replaces gen_ham / V_sk / V_term / onsite of

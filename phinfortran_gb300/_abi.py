@@ -100,6 +100,12 @@ SIGNATURES = {
                                              C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
                                              C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_size_t, C.c_void_p]),
+    "pf_tc_last_error": (C.c_char_p, []),
+    "pf_tc_zgemm_workspace_size": (C.c_size_t, [C.c_int] * 6),
+    "pf_tc_zgemm_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                  C.c_void_p, C.c_int, C.c_longlong, C.c_void_p, C.c_int, C.c_longlong,
+                                  C.c_double, C.c_void_p, C.c_int, C.c_longlong, C.c_int,
+                                  C.c_void_p, C.c_size_t, C.c_void_p]),
     "pf_fullh_last_error": (C.c_char_p, []),
     "pf_gen_dyn": (C.c_int, [C.c_int] * 7 + [_dp, _ip, C.c_int, _ip, _dp, _dp, _dp, C.c_int, _dp, C.c_int, _dp]),
     "pf_gen_dyn_dev": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_int] + [C.c_void_p] * 7

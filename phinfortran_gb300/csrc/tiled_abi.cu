@@ -12,9 +12,11 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/phinfortran_gb300.h"
+#include "tc_gemm.h"
 #include "tiled.cuh"
 #include "transport.cuh"
 
@@ -236,7 +238,7 @@ struct TLayout {
 
 size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-TLayout tlayout(int n, int nl, int nr, int npts, size_t cxb) {
+TLayout tlayout(int n, int nl, int nr, int npts, size_t cxb, bool tc = false) {
   TLayout l;
   l.n = n;
   l.nl = nl;
@@ -246,7 +248,8 @@ TLayout tlayout(int n, int nl, int nr, int npts, size_t cxb) {
   int nb = 32;
   while (nb > 4 && ((size_t)l.m * nb + l.m) * cxb > kPanelBytes) nb >>= 1;
   l.nb = nb;
-  const size_t per_point = (kMats * l.mat + 2 * (size_t)l.m * nb + (size_t)nb * nb + 8) * cxb + (size_t)l.m * 4 + 64;
+  size_t per_point = (kMats * l.mat + 2 * (size_t)l.m * nb + (size_t)nb * nb + 8) * cxb + (size_t)l.m * 4 + 64;
+  if (tc) per_point += pf::tc::zgemm_workspace(l.m, l.m, l.m, 1, false, false);
   size_t b = kBatchBytes / per_point;
   if (b < 1) b = 1;
   if (b > (size_t)kMaxBatch) b = kMaxBatch;
@@ -308,6 +311,12 @@ struct Engine {
   TLayout L;
   Work<T> w;
   int* host_count;
+  // tensor-core products (FP64 engine only): slice workspace and the
+  // product kernel's error flag
+  bool tc = false;
+  void* tcw = nullptr;
+  size_t tcw_bytes = 0;
+  int* tcerr = nullptr;
 
   dim3 eg(int elems) const { return dim3((elems + 255) / 256, B); }
 
@@ -316,6 +325,35 @@ struct Engine {
                    const int* active, const cx<T>* zdiag = nullptr, const cx<T>* H = nullptr, int ldh = 0,
                    long long sH = 0) {
     if (m <= 0 || n <= 0) return cudaSuccess;
+    if constexpr (std::is_same<T, double>::value) {
+      if (tc) {
+        if (alpha.y != 0.0 || beta.y != 0.0) return cudaErrorInvalidValue;
+        pf::tc::ZgemmArgs a{};
+        a.m = m;
+        a.n = n;
+        a.k = k;
+        a.A = A;
+        a.lda = lda;
+        a.sA = sA;
+        a.ca = ca;
+        a.B = Bm;
+        a.ldb = ldb;
+        a.sB = sB;
+        a.cb = cb;
+        a.C = C;
+        a.ldc = ldc;
+        a.sC = sC;
+        a.alpha = alpha.x;
+        a.beta = beta.x;
+        a.batch = B;
+        a.active = active;
+        a.zdiag = zdiag;
+        a.H = H;
+        a.ldh = ldh;
+        a.sH = sH;
+        return pf::tc::zgemm(a, tcw, tcw_bytes, tcerr, s);
+      }
+    }
     GemmArgs<T> g;
     g.m = m;
     g.n = n;
@@ -534,13 +572,24 @@ int drive(int n, int nl, int nr, int L, int nq, const double* const blk[8], int 
           int max_iter, double* transl, int* status, int* iters, char* base, size_t work_bytes, cudaStream_t st,
           int arith) {
   Engine<T> e;
-  e.L = tlayout(n, nl, nr, npts, sizeof(cx<T>));
+  const bool tc = arith == PF_ARITH_TC;
+  e.L = tlayout(n, nl, nr, npts, sizeof(cx<T>), tc);
   const size_t cb = conv_bytes(n, nl, nr, L, arith);
-  const size_t need = 256 + cb + carve<T>(nullptr, e.L, &e.w);
+  const size_t tcb = tc ? pf::tc::zgemm_workspace(e.L.m, e.L.m, e.L.m, e.L.batch, false, false) : 0;
+  const size_t need = 256 + cb + carve<T>(nullptr, e.L, &e.w) + tcb;
   if (!base || work_bytes < need) return set_err(PF_ERR_ARG, "pf_tiled: workspace too small");
-  int* mirror_dev = reinterpret_cast<int*>(base);  // 256-byte header
+  if (tc && !pf::tc::tma_available())
+    return set_err(PF_ERR_CUDA, "pf_tiled: the driver provides no cuTensorMapEncodeTiled");
+  int* mirror_dev = reinterpret_cast<int*>(base);  // 256-byte header: mirror flag, tensor-core error flag
   pf::df64* conv = reinterpret_cast<pf::df64*>(base + 256);
-  carve<T>(base + 256 + cb, e.L, &e.w);
+  const size_t wb = carve<T>(base + 256 + cb, e.L, &e.w);
+  if (tc) {
+    e.tc = true;
+    e.tcw = base + 256 + cb + wb;
+    e.tcw_bytes = tcb;
+    e.tcerr = mirror_dev + 1;
+    TL_CUDA(cudaMemsetAsync(e.tcerr, 0, sizeof(int), st));
+  }
   e.s = st;
   int host_count = 0;
   e.host_count = &host_count;
@@ -615,6 +664,11 @@ int drive(int n, int nl, int nr, int L, int nq, const double* const blk[8], int 
     i0 = i1;
   }
   TL_CUDA(cudaStreamSynchronize(st));
+  if (tc) {
+    int herr = 0;
+    TL_CUDA(cudaMemcpy(&herr, e.tcerr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) return set_err(PF_ERR_CUDA, "pf_tiled: a pipeline wait of the tensor-core product kernel timed out");
+  }
   return PF_SUCCESS;
 }
 
@@ -627,12 +681,14 @@ const char* pf_tiled_last_error(void) { return g_err; }
 size_t pf_transport_tdb_tiled_workspace_size(int n, int nl, int nr, int L, int nq, int npts, int arith) {
   if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0) return 0;
   if (n > PF_NMAX_TILED || nl > PF_NMAX_TILED || nr > PF_NMAX_TILED) return 0;
-  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64) return 0;
-  const TLayout L2 = tlayout(n, nl, nr, npts, 16);
+  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64 && arith != PF_ARITH_TC) return 0;
+  const TLayout L2 = tlayout(n, nl, nr, npts, 16, arith == PF_ARITH_TC);
   const size_t cb = conv_bytes(n, nl, nr, L, arith);
-  if (arith == PF_ARITH_FP64) {
+  if (arith != PF_ARITH_DF64) {
     Work<double> w;
-    return 256 + cb + carve<double>(nullptr, L2, &w);
+    const size_t tcb =
+        arith == PF_ARITH_TC ? pf::tc::zgemm_workspace(L2.m, L2.m, L2.m, L2.batch, false, false) : 0;
+    return 256 + cb + carve<double>(nullptr, L2, &w) + tcb;
   }
   Work<pf::df64> w;
   return 256 + cb + carve<pf::df64>(nullptr, L2, &w);
@@ -652,12 +708,13 @@ int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq, const doubl
     return set_err(PF_ERR_ARG, "pf_tiled: null block pointer");
   if (!E || !transl || !status) return set_err(PF_ERR_ARG, "pf_tiled: null pointer");
   if (max_iter <= 0) return set_err(PF_ERR_ARG, "pf_tiled: max_iter must be positive");
-  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64) return set_err(PF_ERR_ARG, "pf_tiled: unknown arithmetic");
+  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64 && arith != PF_ARITH_TC)
+    return set_err(PF_ERR_ARG, "pf_tiled: unknown arithmetic");
   if (npts == 0) return PF_SUCCESS;
   const double* blk[8] = {HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd};
   cudaStream_t st = (cudaStream_t)stream;
   char* base = reinterpret_cast<char*>(work);
-  if (arith == PF_ARITH_FP64)
+  if (arith != PF_ARITH_DF64)
     return drive<double>(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence,
                          max_iter, transl, status, iters, base, work_bytes, st, arith);
   return drive<pf::df64>(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence,

@@ -81,17 +81,21 @@ def _ptr(a, ctype=C.c_double):
 
 
 NMAX_RESIDENT = 48   # PF_NMAX_RESIDENT
+# precision -> arith of the large-block entry (PF_ARITH_FP64 / _DF64 / _TC)
+TILED_ARITH = {"fp64": 0, "df64": 1, "tc": 2, "mixed": 2}
 
 
 def _transport_tiled(E, nq, dims, arrs, *, eta, eta0, convergence, dev_factor, qidx, zero_flag, max_iter,
                      want_transr, check, precision):
     """Blocks above the resident size: pf_transport_tdb_tiled_dev on torch
-    device buffers (T_L only).  precision "mixed" selects the double-float
-    arithmetic of the tiled engine (FP32 pipe, ~48-bit)."""
+    device buffers (T_L only).  precision: "fp64" (SIMT FP64 block
+    products), "tc" (the FP64 algorithm with every block product on the
+    tensor cores as exact BF16 slice products), "df64" (double-float
+    arithmetic on the FP32 pipe, ~48-bit); "mixed" selects "tc"."""
     import torch
     if want_transr:
         raise ValueError("T_R is not computed for blocks above 48 (pass want_transr=False)")
-    arith = 0 if precision == "fp64" else 1   # PF_ARITH_FP64 / PF_ARITH_DF64
+    arith = TILED_ARITH[precision]
     lib = _abi.load()
     n, nl, nr, L = dims
     dev = {k: torch.from_numpy(fortran_block(v).copy()).cuda() for k, v in arrs.items()}
@@ -133,14 +137,19 @@ def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=No
     double-float leads, FP32 factorisation, double-float refinement: one
     sweep for every point and up to `refine_iters` - 1 more for the points
     whose last correction of G_{0,N+1} was above 3e-5 relative; T_L only).
+    Blocks above 48 go through the large-block entry, where "mixed" (or
+    "tc") puts the block products on the tensor cores and "df64" selects
+    the double-float engine.
     Returns dict(transl, transr, status, iters).
     """
-    if precision not in ("fp64", "mixed"):
-        raise ValueError("precision must be 'fp64' or 'mixed'")
+    if precision not in TILED_ARITH:
+        raise ValueError("precision must be 'fp64', 'mixed', 'tc' or 'df64'")
     lib = _abi.load()
     if isinstance(blocks, dict):
         blocks = TdbBlocks.from_dict(blocks)
     nq, (n, nl, nr, L), arrs = blocks.stacked()
+    if max(n, nl, nr) <= NMAX_RESIDENT and precision in ("tc", "df64"):
+        raise ValueError("precision 'tc' and 'df64' are large-block (n > 48) arithmetics")
     if max(n, nl, nr) > NMAX_RESIDENT:
         return _transport_tiled(E, nq, (n, nl, nr, L), arrs, eta=eta, eta0=eta0, convergence=convergence,
                                 dev_factor=dev_factor, qidx=qidx, zero_flag=zero_flag, max_iter=max_iter,
@@ -227,6 +236,26 @@ class DeviceTransport:
         self.transr = torch.zeros(npts_max, dtype=torch.float64, device=device)
         self.status = torch.zeros(npts_max, dtype=torch.int32, device=device)
         self.iters = torch.zeros((npts_max, 2), dtype=torch.int32, device=device)
+
+    def capture(self, E, qidx=None, zero_flag=None):
+        """Record one ``run`` on these device-resident inputs into a CUDA
+        graph and return it (``g.replay()`` re-runs the whole batched pass --
+        block conversions, lead decimations, factorisation, refinement
+        sweeps, Caroli traces -- with no host work; the outputs land in
+        ``transl`` / ``status`` / ``iters`` as after ``run``).  The C entry
+        is stream-ordered with no host synchronisation, so it captures as is;
+        one uncaptured run first sets the kernels' attributes."""
+        torch = self.torch
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self.run(E, qidx, zero_flag, stream=side)
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, capture_error_mode="thread_local"):
+            self.run(E, qidx, zero_flag, stream=torch.cuda.current_stream())
+        return g
 
     def run(self, E, qidx=None, zero_flag=None, stream=None):
         torch = self.torch

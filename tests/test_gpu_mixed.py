@@ -91,3 +91,24 @@ def test_mixed_edge_shapes(cuda_ready):
                           precision="mixed", refine_iters=2)
         o = N.transport(E, blocks, 0.0, 1e-3, 1e-12, 1.0)
         assert np.abs(r["transl"] - o["transl"]).max() < 1e-9, L
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_graph_replay_matches_direct_run(cuda_ready, precision):
+    """The batched pass captured into a CUDA graph and replayed gives the
+    direct run's T bit for bit (same kernels, same order)."""
+    import torch
+    from phinfortran_gb300 import DeviceTransport
+    b, E, p = S.tb_ribbon(W=24, L=40, ne=96)
+    Ed = torch.from_numpy(E).cuda()
+    dt = DeviceTransport(b, E.size, precision=precision, **p)
+    dt.run(Ed)
+    torch.cuda.synchronize()
+    T0 = dt.transl[:E.size].cpu().numpy().copy()
+    g = dt.capture(Ed)
+    dt.transl.zero_()
+    for _ in range(2):
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(dt.transl[:E.size].cpu().numpy(), T0)
+        assert (dt.status[:E.size].cpu().numpy() == 0).all()

@@ -79,9 +79,33 @@ def test_tiled_diamond_blocked(cuda_ready):
 
 @pytest.mark.parametrize("nc,kp", [(2, 27), (3, 9)])
 def test_tiled_double_float(cuda_ready, nc, kp):
-    """precision="mixed" above 48: the tiled engine in double-float
+    """precision="df64" above 48: the tiled engine in double-float
     arithmetic (FP32 pipe); T within 1e-8 of the FP64 oracle (n = 96 and the
     blocked inverse at n = 216)."""
     b, E, p, aux = S.diamond_phonon(nc=nc, L=4, nk_side=8, ne=12, kpoints=[kp], block=2)
     bq = {k: v[0] for k, v in b.items()}
-    check_against_oracle(bq, E[2:11:2], p, tol=1e-8, precision="mixed")
+    check_against_oracle(bq, E[2:11:2], p, tol=1e-8, precision="df64")
+
+
+@pytest.mark.parametrize("case", ["sc108", "sc147", "diamond96", "diamond216"])
+def test_tiled_tensor_core(cuda_ready, case):
+    """precision="tc": the FP64 algorithm with every block product on the
+    tcgen05 tensor cores (exact BF16 slice products assembled in FP64); the
+    FP64 oracle's T within 1e-9 and its decimation counts within 1, for the
+    shared-memory inverse (n = 96, 108) and the blocked inverse whose
+    trailing updates are tensor-core products (n = 147, 216)."""
+    if case == "sc108":
+        b, E, p, _ = S.sc_phonon(nx=6, ny=6, L=5, ne=20, seed_index=11)
+        check_against_oracle(b, E[1:], p, precision="tc")
+    elif case == "sc147":
+        b, E, p, _ = S.sc_phonon(nx=7, ny=7, L=3, ne=10, seed_index=12)
+        check_against_oracle(b, E[1:], p, precision="tc")
+    elif case == "diamond96":
+        b, E, p, aux = S.diamond_phonon(nc=2, L=6, nk_side=8, ne=24, kpoints=[5, 27], block=3)
+        Es = E[2:22:3]
+        q = np.repeat(np.arange(2, dtype=np.int32), Es.size)
+        check_against_oracle(b, np.tile(Es, 2), p, qidx=q, precision="tc")
+    else:
+        b, E, p, aux = S.diamond_phonon(nc=3, L=3, nk_side=8, ne=12, kpoints=[9], block=2)
+        bq = {k: v[0] for k, v in b.items()}
+        check_against_oracle(bq, E[3:9:2], p, precision="tc")
