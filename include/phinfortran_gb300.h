@@ -120,8 +120,15 @@ int pf_transport_tdb(int n, int nl, int nr, int L, int nq,
 /*
  * Mixed-precision transport (T_L only), device pointers.  Same inputs and
  * meaning as pf_transport_tdb_dev; the arithmetic differs:
- *   - both lead decimations run in double-float (pairs of FP32 numbers,
- *     ~48-bit significand) -- the FP64 algorithm of negf/surface.f90:488-497;
+ *   - both lead decimations run in FP64 (negf/surface.f90:488-497): a
+ *     Lopez-Sancho step doubles the relative error of its couplings, so near
+ *     subband edges at eta ~ 1e-6 a 48-bit decimation leaves T up to 5e-8
+ *     away from FP64; pf_transport_tdb_mixed_ex_dev can select double-float
+ *     decimations (pairs of FP32 numbers on the FP32 pipe, faster, ~48-bit);
+ *     for 256 points or more the batch is split into chunks that alternate
+ *     between `stream` and a second stream of the library, so one chunk's
+ *     FP64 decimations overlap the FP32 factorisation of another (the call
+ *     stays ordered with respect to `stream`);
  *   - the device blocks are factorised in FP32 (the left-connected
  *     recursion of negf/lesser.f90:547-654 as a block LU of the extended
  *     lead+device matrix), and the last block column G_{:,N+1} is refined
@@ -148,6 +155,24 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq,
                                int refine_iters, double* transl, int* status,
                                int* iters, void* work, size_t work_bytes,
                                void* stream);
+
+/*
+ * pf_transport_tdb_mixed_dev with the lead arithmetic chosen by lead_arith:
+ * PF_ARITH_FP64 (what pf_transport_tdb_mixed_dev does) or PF_ARITH_DF64
+ * (double-float decimations, one stream).  Same workspace size.
+ */
+int pf_transport_tdb_mixed_ex_dev(int n, int nl, int nr, int L, int nq,
+                                  const double* HL, const double* HLv,
+                                  const double* HR, const double* HRv,
+                                  const double* Hd, const double* Hdv,
+                                  const double* Hld, const double* Hrd,
+                                  int npts, const double* E, const int* qidx,
+                                  const int* zero_flag,
+                                  double eta, double eta0, double dev_factor,
+                                  double convergence, int max_iter,
+                                  int refine_iters, int lead_arith,
+                                  double* transl, int* status, int* iters,
+                                  void* work, size_t work_bytes, void* stream);
 
 /* Host-pointer variant of pf_transport_tdb_mixed_dev (synchronous). */
 int pf_transport_tdb_mixed(int n, int nl, int nr, int L, int nq,

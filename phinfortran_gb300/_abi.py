@@ -36,6 +36,14 @@ SIGNATURES = {
                                              C.c_int, C.c_int,
                                              C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_size_t, C.c_void_p]),
+    "pf_transport_tdb_mixed_ex_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_double, C.c_double, C.c_double, C.c_double,
+                                                C.c_int, C.c_int, C.c_int,
+                                                C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_size_t, C.c_void_p]),
     "pf_transport_tdb_mixed": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                          _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                          C.c_int, _dp, _ip, _ip,

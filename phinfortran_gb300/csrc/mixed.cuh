@@ -62,6 +62,10 @@ struct MSys {
   // used when *ell_overflow == 0 (every row of every block has <= K nonzeros)
   Ell eHd, eHdv, eHdvH, eHld, eHldH, eHrd, eHrdH;
   const int* ell_overflow;
+  // FP64 lead blocks (the caller's arrays) and the lead arithmetic:
+  // lead_fp64 != 0 runs the decimations in FP64 (the default), else df64
+  const cx<double> *dHL, *dHLv, *dHR, *dHRv;
+  int lead_fp64;
 };
 
 enum { NSM_M = 6 };
@@ -145,14 +149,91 @@ struct EpiRes0 {
   }
 };
 
+// dst (type A) = src (type B) or its conjugate transpose, through FP64
+template <typename A, typename B>
+__device__ void copy_cvt(cx<A>* dst, int ldd, bool conj_t, const cx<B>* src, int lds, int m, int n) {
+  for (int i = threadIdx.x; i < m * n; i += blockDim.x) {
+    const int r = i % m, c = i / m;
+    const cx<B> v = conj_t ? cconj(src[c + r * lds]) : src[r + c * lds];
+    cx<A> o;
+    o.x = conv<A>(to_d(v.x));
+    o.y = conv<A>(to_d(v.y));
+    dst[r + (size_t)c * ldd] = o;
+  }
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
-// Lead decimations in df64.  Results left in per-CTA scratch:
+// Lead decimations in FP64 (the algorithm and arithmetic of the plain FP64
+// path, negf/surface.f90:488-497), results converted to the layouts of the
+// df64 variant below.  The decimation is the part of the mixed pipeline
+// that double-float cannot carry at eta ~ 1e-6: a Lopez-Sancho step doubles
+// the relative error of alpha and beta, so a rounding error made early is
+// amplified by 2^(remaining steps) -- up to ~2^20 near subband edges, where
+// the doubling phase lasts until 2^i ~ 1/eta.  With 48-bit leads 0.7 % of
+// the ribbon's FP64-reproducible energies ended 1e-8 .. 5e-8 away from FP64;
+// with FP64 leads every energy is within 2.2e-9.  The CTA's df64-sized
+// slots hold the FP64 matrices (both 16 bytes per complex element).
+// ---------------------------------------------------------------------------
+template <int S>
+__device__ int mixed_leads64(const MCtx& mc, const MSys& sys, int q, double E, const Params& P, int* it_l,
+                             int* it_r) {
+  Ctx<double> c;
+  for (int i = 0; i < NSM; ++i) c.sm[i] = reinterpret_cast<cx<double>*>(mc.sm[i]);
+  c.gs[G_E1] = reinterpret_cast<cx<double>*>(mc.gs[M_E1]);
+  c.gs[G_ES] = reinterpret_cast<cx<double>*>(mc.gs[M_ES]);
+  c.gs[G_W2] = reinterpret_cast<cx<double>*>(mc.gs[M_W2]);
+  c.gs[G_W3] = reinterpret_cast<cx<double>*>(mc.gs[M_W3]);
+  c.ld = mc.ld;
+  c.iw.rowk = reinterpret_cast<cx<double>*>(mc.iwd.rowk);
+  c.iw.colk = reinterpret_cast<cx<double>*>(mc.iwd.colk);
+  c.iw.perm = mc.iwd.perm;
+  c.iw.flag = mc.iwd.flag;
+  c.red = mc.red;
+  const int ld = mc.ld, nl = sys.nl, nr = sys.nr;
+  const double eps = E * P.eta + P.eta0;
+  int st = PF_OK;
+  cx<double>* tmp = reinterpret_cast<cx<double>*>(mc.gs[M_W2]);
+  {
+    const cx<double>* HL = sys.dHL + (size_t)q * nl * nl;
+    const cx<double>* HLv = sys.dHLv + (size_t)q * nl * nl;
+    st |= decimate<double, S>(c, nl, mk<double>(E, -eps), opN<double>(HL, nl), opC<double>(HLv, nl),
+                              opN<double>(HLv, nl), P.convergence, P.max_iter, it_l);
+    copy_cvt<float, double>(mc.lu, ld, true, c.sm[2], ld, nl, nl);             // g_0 = g_adv^H
+    copy_cvt<df64, double>(mc.gs[M_ESL], ld, true, c.gs[G_ES], ld, nl, nl);    // es_adv^H
+    lead_sigma<double, S>(c, nl, HLv);                                         // SM1 = sl_adv
+    gamma_from_sigma(tmp, ld, c.sm[1], ld, nl, -1);
+    copy_cvt<df64, double>(mc.gs[M_GML], ld, false, tmp, ld, nl, nl);
+  }
+  if (P.lead_mirror && P.lead_mirror[q]) {
+    copy_cvt<df64, double>(mc.gs[M_SR], ld, true, c.sm[1], ld, nl, nl);
+    copy_cvt<float, double>(mc.fsr, ld, true, c.sm[1], ld, nl, nl);
+    copy_out(mc.gs[M_GMR], ld, false, mc.gs[M_GML], ld, nl, nl);
+    if (it_r) *it_r = *it_l;
+  } else {
+    const cx<double>* HR = sys.dHR + (size_t)q * nr * nr;
+    const cx<double>* HRv = sys.dHRv + (size_t)q * nr * nr;
+    st |= decimate<double, S>(c, nr, mk<double>(E, eps), opN<double>(HR, nr), opC<double>(HRv, nr),
+                              opN<double>(HRv, nr), P.convergence, P.max_iter, it_r);
+    lead_sigma<double, S>(c, nr, HRv);                                         // SM1 = sr_ret
+    copy_cvt<df64, double>(mc.gs[M_SR], ld, false, c.sm[1], ld, nr, nr);
+    copy_cvt<float, double>(mc.fsr, ld, false, c.sm[1], ld, nr, nr);
+    gamma_from_sigma(tmp, ld, c.sm[1], ld, nr, +1);
+    copy_cvt<df64, double>(mc.gs[M_GMR], ld, false, tmp, ld, nr, nr);
+  }
+  return st;
+}
+
+// ---------------------------------------------------------------------------
+// Lead decimations in df64 (or FP64 when sys.lead_fp64).  Results left in
+// per-CTA scratch:
 //   M_ESL = es_adv^H (df64), M_GML = -gml_adv, M_GMR = gmr_ret, M_SR = sr_ret,
 //   lu[0] = gl_ret = g_adv^H (FP32), fsr = FP32 sr_ret.
 // ---------------------------------------------------------------------------
 template <int S>
 __device__ int mixed_leads(const MCtx& mc, const MSys& sys, int q, double E, const Params& P, int* it_l,
                            int* it_r) {
+  if (sys.lead_fp64) return mixed_leads64<S>(mc, sys, q, E, P, it_l, it_r);
   Ctx<df64> c;
   for (int i = 0; i < NSM; ++i) c.sm[i] = mc.sm[i];
   c.gs[G_E1] = mc.gs[M_E1];

@@ -14,11 +14,14 @@
 //     truncated to a 56-bit integer F (integer operations on the FP64 bits);
 //   * slice s = 1..8 holds q_s * 2^-7s with q_s the s-th 7-bit group of F
 //     (|q_s| <= 127: exact in BF16), so x = sum_s q_s 2^-7s + O(2^-56);
-//   * the product keeps the slice pairs with s + t <= 9.  For s + t <= 5 the
+//   * the product keeps the slice pairs with s + t <= 9.  For s + t <= 6 the
 //     FP32 tensor-core sums over K chunks of 256 are integers below 2^22
 //     (127^2 * 256 < 2^22), hence exact; each chunk is drained from TMEM and
-//     added into a 64-bit fixed-point sum.  The pairs with s + t >= 6 weigh
-//     at most 2^-42 and share one FP32 accumulator over the whole K.
+//     added into a 64-bit fixed-point sum.  The pairs with s + t >= 7 weigh
+//     at most 2^-49 and share one FP32 accumulator over the whole K (the
+//     tensor cores' FP32 sums are not correctly rounded, so a heavier
+//     inexact chain would lose accuracy: with s + t >= 6 in it the products
+//     drifted by ~2^-42 relative).
 // The result is assembled in FP64 once per output element and scaled back
 // by 2^(e_row + e_col).  Relative to |A| |B| the error is O(K 2^-55), the
 // accuracy of an FP64 GEMM.
@@ -61,6 +64,9 @@ static_assert(kTmemCols >= 32 && (kTmemCols & (kTmemCols - 1)) == 0, "TMEM alloc
 static_assert(kChunk * 127 * 127 < (1 << 22), "exact chain bound");
 static_assert(kSlices * kBeta == 56, "56-bit fixed point");
 static_assert(kSlices + 1 > kTopD, "the low accumulator receives at least one pair per chunk");
+static_assert(kTopD * kBeta == 42, "fixed-point LSB used in the epilogue");
+// |F| <= chunks * (2^22 << 7 (kTopD - 2)) * pairs: with K <= 4096 (16 chunks) below 2^63
+static_assert(22 + kBeta * (kTopD - 2) + 4 + 4 < 63, "64-bit fixed-point range");
 
 // ---------------------------------------------------------------------------
 // PTX wrappers
@@ -420,7 +426,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         if (ea == kExpBad || eb == kExpBad) {
           v = __longlong_as_double(0x7FF8000000000000ll);
         } else {
-          const double top = (double)F[q * 16 + j] * 0x1p-35;
+          const double top = (double)F[q * 16 + j] * 0x1p-42;  // LSB 2^(-7 kTopD)
           v = scalbn(top + (double)__uint_as_float(r[j]), ea + eb);
         }
         v *= p.alpha;

@@ -18,10 +18,13 @@ namespace tc {
 // Bits per slice, slices per operand, and the largest pair sum s + t (1-based)
 // whose products are accumulated exactly and drained into a 64-bit fixed
 // point sum; pairs with s + t > kTopD go into one FP32 accumulator (their
-// weight is at most 2^-42 of the leading pair's).
+// weight is at most 2^-49 of the leading pair's).  The tensor cores' FP32
+// sums are not correctly rounded: a long chain of small addends drifts by
+// about 2^-40 of the accumulator (measured), so only pairs that light may
+// share the inexact accumulator.
 constexpr int kBeta = 7;
 constexpr int kSlices = 8;
-constexpr int kTopD = 5;
+constexpr int kTopD = 6;
 constexpr int kBM = 128;     // rows of the real product per CTA (TMEM lanes)
 constexpr int kBN = 64;      // columns per CTA
 constexpr int kKStep = 64;   // K per TMA box (one 128-byte swizzle row of BF16)

@@ -190,7 +190,8 @@ class DeviceTransport:
     """
 
     def __init__(self, blocks, npts_max, *, eta, eta0, convergence, dev_factor=10.0,
-                 max_iter=1000, want_transr=False, device="cuda", precision="fp64", refine_iters=2):
+                 max_iter=1000, want_transr=False, device="cuda", precision="fp64", refine_iters=2,
+                 lead_arith="fp64"):
         import torch
         if isinstance(blocks, dict):
             blocks = TdbBlocks.from_dict(blocks)
@@ -198,7 +199,7 @@ class DeviceTransport:
         dev = {k: torch.from_numpy(fortran_block(v).copy()).to(device) for k, v in arrs.items()}
         self._setup(dev, (n, nl, nr, L, nq), npts_max, eta=eta, eta0=eta0, convergence=convergence,
                     dev_factor=dev_factor, max_iter=max_iter, want_transr=want_transr, device=device,
-                    precision=precision, refine_iters=refine_iters)
+                    precision=precision, refine_iters=refine_iters, lead_arith=lead_arith)
 
     @classmethod
     def from_device(cls, dev, dims, npts_max, **kw):
@@ -210,7 +211,7 @@ class DeviceTransport:
         return obj
 
     def _setup(self, dev, dims, npts_max, *, eta, eta0, convergence, dev_factor=10.0, max_iter=1000,
-               want_transr=False, device="cuda", precision="fp64", refine_iters=2):
+               want_transr=False, device="cuda", precision="fp64", refine_iters=2, lead_arith="fp64"):
         import torch
         self.torch = torch
         lib = _abi.load()
@@ -221,6 +222,9 @@ class DeviceTransport:
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.precision = precision
         self.refine_iters = int(refine_iters)
+        if lead_arith not in ("fp64", "df64"):
+            raise ValueError("lead_arith must be 'fp64' or 'df64'")
+        self.lead_arith = 0 if lead_arith == "fp64" else 1   # PF_ARITH_FP64 / PF_ARITH_DF64
         if precision == "mixed":
             want_transr = False
         self.params = (eta, eta0, dev_factor, convergence, max_iter, int(bool(want_transr)))
@@ -276,9 +280,9 @@ class DeviceTransport:
                 self.transl.data_ptr(), self.transr.data_ptr(), self.status.data_ptr(), self.iters.data_ptr(),
                 self.work.data_ptr(), self.work.numel(), C.c_void_p(s.cuda_stream))
         else:
-            rc = lib.pf_transport_tdb_mixed_dev(
+            rc = lib.pf_transport_tdb_mixed_ex_dev(
                 n, nl, nr, L, nq, *[d[k].data_ptr() for k in BLOCK_NAMES], npts, E.data_ptr(), qp, zp,
-                eta, eta0, dev_factor, conv, max_iter, self.refine_iters,
+                eta, eta0, dev_factor, conv, max_iter, self.refine_iters, self.lead_arith,
                 self.transl.data_ptr(), self.status.data_ptr(), self.iters.data_ptr(),
                 self.work.data_ptr(), self.work.numel(), C.c_void_p(s.cuda_stream))
         _abi.check(rc)

@@ -93,13 +93,15 @@ def test_mixed_edge_shapes(cuda_ready):
         assert np.abs(r["transl"] - o["transl"]).max() < 1e-9, L
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_graph_replay_matches_direct_run(cuda_ready, precision):
+@pytest.mark.parametrize("precision,ne", [("fp64", 96), ("mixed", 96), ("mixed", 300)])
+def test_graph_replay_matches_direct_run(cuda_ready, precision, ne):
     """The batched pass captured into a CUDA graph and replayed gives the
-    direct run's T bit for bit (same kernels, same order)."""
+    direct run's T bit for bit (same kernels, same order); with 300 points
+    the mixed path splits the batch over two streams, which the capture
+    records as a fork and a join."""
     import torch
     from phinfortran_gb300 import DeviceTransport
-    b, E, p = S.tb_ribbon(W=24, L=40, ne=96)
+    b, E, p = S.tb_ribbon(W=24, L=40, ne=ne)
     Ed = torch.from_numpy(E).cuda()
     dt = DeviceTransport(b, E.size, precision=precision, **p)
     dt.run(Ed)
@@ -112,3 +114,28 @@ def test_graph_replay_matches_direct_run(cuda_ready, precision):
         torch.cuda.synchronize()
         assert np.array_equal(dt.transl[:E.size].cpu().numpy(), T0)
         assert (dt.status[:E.size].cpu().numpy() == 0).all()
+
+
+def test_fp64_leads_meet_1e8_on_the_ribbon(cuda_ready):
+    """The default mixed path (FP64 lead decimations, FP32 factorisation,
+    double-float refinement) against the FP64 path on 512 energies of the
+    disordered 32-wide ribbon (L = 100, eta = 1e-6): every point within 1e-8
+    relative (|T - T64| / max(|T64|, 1e-3)), through the two-stream chunked
+    schedule; the double-float leads of pf_transport_tdb_mixed_ex_dev stay
+    within 1e-6."""
+    import torch
+    from phinfortran_gb300 import DeviceTransport
+    b, E, p = S.tb_ribbon(W=32, L=100, ne=512)
+    Ed = torch.from_numpy(E).cuda()
+    f64 = DeviceTransport(b, E.size, precision="fp64", **p)
+    f64.run(Ed)
+    mix = DeviceTransport(b, E.size, precision="mixed", **p)
+    mix.run(Ed)
+    d64 = DeviceTransport(b, E.size, precision="mixed", lead_arith="df64", **p)
+    d64.run(Ed)
+    torch.cuda.synchronize()
+    T64 = f64.transl[:E.size].cpu().numpy()
+    assert (mix.status[:E.size].cpu().numpy() == 0).all()
+    r = rel(mix.transl[:E.size].cpu().numpy(), T64)
+    assert r.max() <= 1e-8, (r.max(), int(np.argmax(r)))
+    assert rel(d64.transl[:E.size].cpu().numpy(), T64).max() < 1e-6
