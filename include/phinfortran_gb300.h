@@ -120,15 +120,13 @@ int pf_transport_tdb(int n, int nl, int nr, int L, int nq,
 /*
  * Mixed-precision transport (T_L only), device pointers.  Same inputs and
  * meaning as pf_transport_tdb_dev; the arithmetic differs:
- *   - both lead decimations run in FP64 (negf/surface.f90:488-497): a
- *     Lopez-Sancho step doubles the relative error of its couplings, so near
- *     subband edges at eta ~ 1e-6 a 48-bit decimation leaves T up to 5e-8
- *     away from FP64; pf_transport_tdb_mixed_ex_dev can select double-float
- *     decimations (pairs of FP32 numbers on the FP32 pipe, faster, ~48-bit);
- *     for 256 points or more the batch is split into chunks that alternate
- *     between `stream` and a second stream of the library, so one chunk's
- *     FP64 decimations overlap the FP32 factorisation of another (the call
- *     stays ordered with respect to `stream`);
+ *   - both lead decimations (negf/surface.f90:488-497) run in FP64: the
+ *     doubling iteration amplifies its own rounding, and near subband edges
+ *     at eta ~ 1e-6 double-float (48-bit) decimations leave T up to 5e-8
+ *     away from FP64 even where FP64 itself is reproducible;
+ *     pf_transport_tdb_mixed_ex_dev selects double-float decimations
+ *     (pairs of FP32 numbers on the FP32 pipe) or split ones (first 8 steps
+ *     FP64, the rest double-float) for speed;
  *   - the device blocks are factorised in FP32 (the left-connected
  *     recursion of negf/lesser.f90:547-654 as a block LU of the extended
  *     lead+device matrix), and the last block column G_{:,N+1} is refined
@@ -158,9 +156,12 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq,
 
 /*
  * pf_transport_tdb_mixed_dev with the lead arithmetic chosen by lead_arith:
- * PF_ARITH_FP64 (what pf_transport_tdb_mixed_dev does) or PF_ARITH_DF64
- * (double-float decimations, one stream).  Same workspace size.
+ * PF_ARITH_FP64 (whole decimations in FP64: what pf_transport_tdb_mixed_dev
+ * does), PF_ARITH_SPLIT (the first 8 decimation steps in FP64, the rest in
+ * double-float) or PF_ARITH_DF64 (whole decimations in double-float).  Same
+ * workspace size.
  */
+#define PF_ARITH_SPLIT 3
 int pf_transport_tdb_mixed_ex_dev(int n, int nl, int nr, int L, int nq,
                                   const double* HL, const double* HLv,
                                   const double* HR, const double* HRv,
@@ -398,6 +399,39 @@ int pf_transport_tdb_modes_permode_dev(int n, int nl, int nr, int L, int nq,
                                        int* mode_bz, double* col_sums,
                                        void* work, size_t work_bytes,
                                        void* stream);
+
+/*
+ * pf_transport_tdb_modes_permode_dev with flags (the three per-mode outputs
+ * may all be null).  PF_MODES_ELECTRON selects the electron normalisation of
+ * tb/velocity_mat.f90 (vel_mat, :222-1560): velocity matrices U^H Gamma U
+ * (:467) and t / r = i V^1/2 U^-1 G U^-H V^1/2 (:1352-1370) with none of
+ * the phonon factors a_z / (2 sqrt(E)) and 2 sqrt(E / (a_z a_z)); those
+ * cancel in t and r for E > 0, and only the electron form is defined for
+ * E <= 0 (energies below the band centre).  lambda_eta is the caller's
+ * (the tb driver uses 1e-3, tb/velocity_mat.f90:355).
+ */
+#define PF_MODES_ELECTRON 1
+
+int pf_transport_tdb_modes_ex_dev(int n, int nl, int nr, int L, int nq,
+                                  const double* HL, const double* HLv,
+                                  const double* HR, const double* HRv,
+                                  const double* Hd, const double* Hdv,
+                                  const double* Hld, const double* Hrd,
+                                  int npts, const double* E,
+                                  const int* qidx, const int* zero_flag,
+                                  double eta, double eta0,
+                                  double dev_factor, double convergence,
+                                  int max_iter, double lambda_eta,
+                                  double a_z_l, double a_z_r, int nshift,
+                                  int stride_l, int nrep_l,
+                                  const double* phase_l, int stride_r,
+                                  int nrep_r, const double* phase_r, int flags,
+                                  double* transl, double* transr,
+                                  double* mode_sums, int* status,
+                                  int* nprop, double* mode_kz,
+                                  int* mode_bz, double* col_sums,
+                                  void* work, size_t work_bytes,
+                                  void* stream);
 
 /* Message for the last error of the mode-resolved entry points. */
 const char* pf_modes_last_error(void);

@@ -63,10 +63,21 @@ struct MSys {
   Ell eHd, eHdv, eHdvH, eHld, eHldH, eHrd, eHrdH;
   const int* ell_overflow;
   // FP64 lead blocks (the caller's arrays) and the lead arithmetic:
-  // lead_fp64 != 0 runs the decimations in FP64 (the default), else df64
+  // PF_LEAD_FP64 whole decimations in FP64, PF_LEAD_DF64 in double-float,
+  // PF_LEAD_SPLIT the first PF_LEAD_FP64_STEPS steps in FP64, the rest in
+  // double-float
   const cx<double> *dHL, *dHLv, *dHR, *dHRv;
-  int lead_fp64;
+  int lead_mode;
 };
+enum { PF_LEAD_FP64 = 0, PF_LEAD_DF64 = 1, PF_LEAD_SPLIT = 2 };
+
+// Lopez-Sancho steps carried in FP64 before the split decimation continues in
+// double-float.  On the disordered 32-wide ribbon (1024 energies, eta 1e-6)
+// the split decimation halves the number of energies whose T misses FP64 by
+// more than 1e-8 (53 instead of 114; 2 instead of 6 among the FP64-
+// reproducible ones); only whole FP64 decimations remove them all, so the
+// split is an option for speed, not the default.
+constexpr int PF_LEAD_FP64_STEPS = 8;
 
 enum { NSM_M = 6 };
 // per-CTA df64 scratch matrices
@@ -167,13 +178,15 @@ __device__ void copy_cvt(cx<A>* dst, int ldd, bool conj_t, const cx<B>* src, int
 // Lead decimations in FP64 (the algorithm and arithmetic of the plain FP64
 // path, negf/surface.f90:488-497), results converted to the layouts of the
 // df64 variant below.  The decimation is the part of the mixed pipeline
-// that double-float cannot carry at eta ~ 1e-6: a Lopez-Sancho step doubles
-// the relative error of alpha and beta, so a rounding error made early is
-// amplified by 2^(remaining steps) -- up to ~2^20 near subband edges, where
-// the doubling phase lasts until 2^i ~ 1/eta.  With 48-bit leads 0.7 % of
-// the ribbon's FP64-reproducible energies ended 1e-8 .. 5e-8 away from FP64;
-// with FP64 leads every energy is within 2.2e-9.  The CTA's df64-sized
-// slots hold the FP64 matrices (both 16 bytes per complex element).
+// that double-float cannot carry at eta ~ 1e-6: with 48-bit decimations 114
+// of the disordered ribbon's 1024 energies end more than 1e-8 from FP64 (6
+// of them FP64-reproducible, up to 4.4e-8), with FP64 decimations every
+// energy is within 2.2e-9.  The doubling iteration amplifies its rounding
+// errors (a relative error of alpha or beta doubles with every step), and a
+// residual of the surface function does not single the bad energies out
+// (FP64 decimations leave residuals up to 2e-7 there too), so every point
+// takes FP64 decimations.  The CTA's df64-sized slots hold the FP64
+// matrices (both 16 bytes per complex element).
 // ---------------------------------------------------------------------------
 template <int S>
 __device__ int mixed_leads64(const MCtx& mc, const MSys& sys, int q, double E, const Params& P, int* it_l,
@@ -224,16 +237,104 @@ __device__ int mixed_leads64(const MCtx& mc, const MSys& sys, int q, double E, c
   return st;
 }
 
+// One Lopez-Sancho step (negf/surface.f90:488-497) on the state in c:
+// alpha = SM0, beta = SM1, e1 = G_E1, es = G_ES; SM2, G_W2, G_W3 scratch.
+template <typename R, int S>
+__device__ int sancho_step(const Ctx<R>& c, int m, cx<R> z) {
+  const int ld = c.ld;
+  cx<R>* al = c.sm[0];
+  cx<R>* be = c.sm[1];
+  cx<R>* W1 = c.sm[2];
+  cx<R>* e1 = c.gs[G_E1];
+  cx<R>* es = c.gs[G_ES];
+  cx<R>* W2 = c.gs[G_W2];
+  cx<R>* W3 = c.gs[G_W3];
+  shift_neg(W1, ld, z, e1, ld, m);                                                              // z - e1
+  const int st = inverse(W1, ld, m, c.iw);                                                      // ive
+  row_gemm<R, S>(m, m, m, opN<R>(al, ld), opN<R>(W1, ld), EpiStore<R>{W2, ld, mk<R>(1, 0)});  // alpha ive
+  row_gemm<R, S>(m, m, m, opN<R>(be, ld), opN<R>(W1, ld), EpiStore<R>{W3, ld, mk<R>(1, 0)});  // beta ive
+  row_gemm<R, S>(m, m, m, opN<R>(W2, ld), opN<R>(be, ld), EpiAcc2<R>{e1, es, ld});
+  row_gemm<R, S>(m, m, m, opN<R>(W3, ld), opN<R>(al, ld), EpiAcc<R>{e1, ld});
+  row_gemm<R, S>(m, m, m, opN<R>(W2, ld), opN<R>(al, ld), EpiStore<R>{W2, ld, mk<R>(1, 0)});
+  row_gemm<R, S>(m, m, m, opN<R>(W3, ld), opN<R>(be, ld), EpiStore<R>{W3, ld, mk<R>(1, 0)});
+  copy_in(al, ld, opN<R>(W2, ld), m, m);
+  copy_in(be, ld, opN<R>(W3, ld), m, m);
+  return st;
+}
+
+// In-place FP64 -> df64 of an m x m slot (both 16 bytes per complex element;
+// every element is read and written by the same thread).
+__device__ void slot_to_df64(dcx* a, int ld, int m) {
+  for (int i = threadIdx.x; i < m * m; i += blockDim.x) {
+    const int r = i % m, c = i / m;
+    const cx<double> v = reinterpret_cast<const cx<double>*>(a)[r + c * ld];
+    a[r + c * ld] = mk<df64>(df64(v.x), df64(v.y));
+  }
+  __syncthreads();
+}
+
+// Split decimation: the FP64 algorithm of negf/surface.f90:479-497 with the
+// first PF_LEAD_FP64_STEPS steps in FP64 and the rest in df64 (the state is
+// converted in place).  On return SM2 holds g = inv(z - es) and G_ES holds
+// es, both df64, as after decimate<df64>.
+template <int S>
+__device__ int decimate_split(const Ctx<df64>& cd, int m, double E, double eps_signed, const cx<double>* h00,
+                              const cx<double>* v, double conv, int max_iter, int* iters_out) {
+  Ctx<double> c;
+  for (int i = 0; i < NSM; ++i) c.sm[i] = reinterpret_cast<cx<double>*>(cd.sm[i]);
+  for (int i : {(int)G_E1, (int)G_ES, (int)G_W2, (int)G_W3}) c.gs[i] = reinterpret_cast<cx<double>*>(cd.gs[i]);
+  c.ld = cd.ld;
+  c.iw.rowk = reinterpret_cast<cx<double>*>(cd.iw.rowk);
+  c.iw.colk = reinterpret_cast<cx<double>*>(cd.iw.colk);
+  c.iw.perm = cd.iw.perm;
+  c.iw.flag = cd.iw.flag;
+  c.red = cd.red;
+  const int ld = cd.ld;
+  copy_in(c.gs[G_E1], ld, opN<double>(h00, m), m, m);
+  copy_in(c.gs[G_ES], ld, opN<double>(h00, m), m, m);
+  copy_in(c.sm[0], ld, opC<double>(v, m), m, m);  // alpha0 = V^H
+  copy_in(c.sm[1], ld, opN<double>(v, m), m, m);  // beta0 = V
+  int st = PF_OK;
+  double maxdiff = max_abs(c.sm[0], ld, m, m, c.red);
+  int it = 0;
+  const cx<double> z64 = mk<double>(E, eps_signed);
+  while (maxdiff > conv && it < PF_LEAD_FP64_STEPS && it < max_iter) {
+    st |= sancho_step<double, S>(c, m, z64);
+    maxdiff = max_abs(c.sm[0], ld, m, m, c.red);
+    ++it;
+  }
+  slot_to_df64(cd.sm[0], ld, m);
+  slot_to_df64(cd.sm[1], ld, m);
+  slot_to_df64(cd.gs[G_E1], ld, m);
+  slot_to_df64(cd.gs[G_ES], ld, m);
+  const dcx z = mk<df64>(df64(E), df64(eps_signed));
+  while (maxdiff > conv) {
+    if (it >= max_iter) {
+      st |= PF_NOT_CONVERGED;
+      break;
+    }
+    st |= sancho_step<df64, S>(cd, m, z);
+    maxdiff = max_abs(cd.sm[0], ld, m, m, cd.red);
+    ++it;
+  }
+  if (maxdiff != maxdiff) st |= PF_NAN;
+  shift_neg(cd.sm[2], ld, z, cd.gs[G_ES], ld, m);
+  st |= inverse(cd.sm[2], ld, m, cd.iw);
+  if (iters_out) *iters_out = it;
+  return st;
+}
+
 // ---------------------------------------------------------------------------
-// Lead decimations in df64 (or FP64 when sys.lead_fp64).  Results left in
-// per-CTA scratch:
+// Lead decimations in df64 (whole or split; FP64 when sys.lead_mode is
+// PF_LEAD_FP64).  Results left in per-CTA scratch:
 //   M_ESL = es_adv^H (df64), M_GML = -gml_adv, M_GMR = gmr_ret, M_SR = sr_ret,
 //   lu[0] = gl_ret = g_adv^H (FP32), fsr = FP32 sr_ret.
 // ---------------------------------------------------------------------------
 template <int S>
 __device__ int mixed_leads(const MCtx& mc, const MSys& sys, int q, double E, const Params& P, int* it_l,
                            int* it_r) {
-  if (sys.lead_fp64) return mixed_leads64<S>(mc, sys, q, E, P, it_l, it_r);
+  if (sys.lead_mode == PF_LEAD_FP64) return mixed_leads64<S>(mc, sys, q, E, P, it_l, it_r);
+  const bool split = sys.lead_mode == PF_LEAD_SPLIT;
   Ctx<df64> c;
   for (int i = 0; i < NSM; ++i) c.sm[i] = mc.sm[i];
   c.gs[G_E1] = mc.gs[M_E1];
@@ -249,8 +350,12 @@ __device__ int mixed_leads(const MCtx& mc, const MSys& sys, int q, double E, con
   {
     const dcx* HL = sys.HL + (size_t)q * nl * nl;
     const dcx* HLv = sys.HLv + (size_t)q * nl * nl;
-    st |= decimate<df64, S>(c, nl, mk<df64>(df64(E), df64(-eps)), opN<df64>(HL, nl), opC<df64>(HLv, nl),
-                            opN<df64>(HLv, nl), P.convergence, P.max_iter, it_l);
+    if (split)
+      st |= decimate_split<S>(c, nl, E, -eps, sys.dHL + (size_t)q * nl * nl, sys.dHLv + (size_t)q * nl * nl,
+                              P.convergence, P.max_iter, it_l);
+    else
+      st |= decimate<df64, S>(c, nl, mk<df64>(df64(E), df64(-eps)), opN<df64>(HL, nl), opC<df64>(HLv, nl),
+                              opN<df64>(HLv, nl), P.convergence, P.max_iter, it_l);
     cvt_df_to_f(mc.lu, ld, true, c.sm[2], ld, nl, nl);          // g_0 = g_adv^H
     copy_out(mc.gs[M_ESL], ld, true, c.gs[G_ES], ld, nl, nl);   // es_adv^H
     lead_sigma<df64, S>(c, nl, HLv);                            // SM1 = sl_adv
@@ -265,8 +370,12 @@ __device__ int mixed_leads(const MCtx& mc, const MSys& sys, int q, double E, con
   } else {
     const dcx* HR = sys.HR + (size_t)q * nr * nr;
     const dcx* HRv = sys.HRv + (size_t)q * nr * nr;
-    st |= decimate<df64, S>(c, nr, mk<df64>(df64(E), df64(eps)), opN<df64>(HR, nr), opC<df64>(HRv, nr),
-                            opN<df64>(HRv, nr), P.convergence, P.max_iter, it_r);
+    if (split)
+      st |= decimate_split<S>(c, nr, E, eps, sys.dHR + (size_t)q * nr * nr, sys.dHRv + (size_t)q * nr * nr,
+                              P.convergence, P.max_iter, it_r);
+    else
+      st |= decimate<df64, S>(c, nr, mk<df64>(df64(E), df64(eps)), opN<df64>(HR, nr), opC<df64>(HRv, nr),
+                              opN<df64>(HRv, nr), P.convergence, P.max_iter, it_r);
     lead_sigma<df64, S>(c, nr, HRv);                            // SM1 = sr_ret
     copy_out(mc.gs[M_SR], ld, false, c.sm[1], ld, nr, nr);
     cvt_df_to_f(mc.fsr, ld, false, c.sm[1], ld, nr, nr);

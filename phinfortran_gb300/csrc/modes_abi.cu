@@ -96,6 +96,11 @@ struct Chunk {
 
 struct ModeGeom {
   double lambda_eta, a_z_l, a_z_r;
+  // electron normalisation (tb/velocity_mat.f90:467, :1352-1370): V = U^H Gamma U
+  // and t = i V^1/2 ... with no a_z / (2 sqrt(E)) and no 2 sqrt(E / a a)
+  // factors; for E > 0 the two scalings cancel in t, r (same sums), and for
+  // E <= 0 only this one is defined
+  int electron;
   int nshift;
   int stride_l, nrep_l, stride_r, nrep_r;
   const cx<double>* phase_l;  // [nq][nshift][nl]
@@ -348,7 +353,7 @@ __global__ void __launch_bounds__(kTaskThreads)
      pf::EpiStore<double>{t.s[2], ld, pf::mk<double>(1, 0)}, S);
   const double az = left ? geo.a_z_l : geo.a_z_r;
   const double sgn = left ? -1.0 : 1.0;
-  const double f = sgn * az / 2.0 / sqrt(E);
+  const double f = geo.electron ? sgn : sgn * az / 2.0 / sqrt(E);
   mm(m, m, m, pf::opC<double>(t.s[3], ld), pf::opN<double>(t.s[2], ld),
      pf::EpiStore<double>{t.s[0], ld, pf::mk<double>(0.0, f)}, S);
   // ---- inv(U^H) (advanced problems) or inv(U) (retarded)
@@ -468,6 +473,8 @@ __global__ void __launch_bounds__(kTaskThreads)
     for (int u = threadIdx.x; u < 4 * out.mm * nsh; u += blockDim.x) o[u] = 0.0;
     __syncthreads();
   }
+  // prefactor of the t / r chains: 2 sqrt(E / (a_row a_col)) (phonons), 1 (electrons)
+  auto cf = [&](double ar, double ac) { return geo.electron ? 1.0 : 2.0 * sqrt(E / ar / ac); };
   auto chain = [&](int rows, int cols, int krow, int kcol, pf::Op<double> X, double cfac) {
     // s0 = Uinv_col Vh_col (cols x cols)
     pf::copy_in(t.s[0], ld, pf::opN<double>(ch.task(lp, kcol, T_UINV), ld), cols, cols);
@@ -489,11 +496,11 @@ __global__ void __launch_bounds__(kTaskThreads)
   };
   if (!zero) {
     // trl = i 2 sqrt(E/azR/azL) Vh_rR Uinv_rR G_D_RL Uinv_aL Vh_aL  -> transr
-    chain(nr, nl, K_RET_R, K_ADV_L, pf::opN<double>(ch.rec(lp, R_GDRL), ld), 2.0 * sqrt(E / geo.a_z_r / geo.a_z_l));
+    chain(nr, nl, K_RET_R, K_ADV_L, pf::opN<double>(ch.rec(lp, R_GDRL), ld), cf(geo.a_z_r, geo.a_z_l));
     split_sums(t.s[0], ld, nr, nl, bz_rr, bz_al, t.red, &sums[2], &sums[3]);
     col_out(1, nr, nl, bz_rr, bz_al);
     // tlr = i 2 sqrt(E/azL/azR) Vh_rL Uinv_rL G_D_LR Uinv_aR Vh_aR  -> transl
-    chain(nl, nr, K_RET_L, K_ADV_R, pf::opN<double>(ch.rec(lp, R_GDLR), ld), 2.0 * sqrt(E / geo.a_z_l / geo.a_z_r));
+    chain(nl, nr, K_RET_L, K_ADV_R, pf::opN<double>(ch.rec(lp, R_GDLR), ld), cf(geo.a_z_l, geo.a_z_r));
     split_sums(t.s[0], ld, nl, nr, bz_rl, bz_ar, t.red, &sums[0], &sums[1]);
     col_out(0, nl, nr, bz_rl, bz_ar);
     // rrr: (G_R - inv(Q_R)), Q_R = z - Hr - Hrv^H gr Hrv - Hrv grm^H Hrv^H
@@ -509,7 +516,7 @@ __global__ void __launch_bounds__(kTaskThreads)
       __syncthreads();
     }
     // the chain reads X before it reuses slot 3? no: X is copied into s1 first
-    chain(nr, nr, K_RET_R, K_ADV_R, pf::opN<double>(t.s[3], ld), 2.0 * sqrt(E / geo.a_z_r / geo.a_z_r));
+    chain(nr, nr, K_RET_R, K_ADV_R, pf::opN<double>(t.s[3], ld), cf(geo.a_z_r, geo.a_z_r));
     split_sums(t.s[0], ld, nr, nr, bz_rr, bz_ar, t.red, &sums[6], &sums[7]);
     col_out(2, nr, nr, bz_rr, bz_ar);
     // rll: (G_L - inv(Q_L)), Q_L = z - Hl - Hlv^H gl^H Hlv - Hlv glp Hlv^H
@@ -524,7 +531,7 @@ __global__ void __launch_bounds__(kTaskThreads)
       }
       __syncthreads();
     }
-    chain(nl, nl, K_RET_L, K_ADV_L, pf::opN<double>(t.s[3], ld), 2.0 * sqrt(E / geo.a_z_l / geo.a_z_l));
+    chain(nl, nl, K_RET_L, K_ADV_L, pf::opN<double>(t.s[3], ld), cf(geo.a_z_l, geo.a_z_l));
     split_sums(t.s[0], ld, nl, nl, bz_rl, bz_al, t.red, &sums[4], &sums[5]);
     col_out(3, nl, nl, bz_rl, bz_al);
   }
@@ -593,16 +600,17 @@ size_t pf_transport_tdb_modes_workspace_size(int n, int nl, int nr, int nq, int 
   return modes_bytes(lay, nq, chunk, grid);
 }
 
-int pf_transport_tdb_modes_permode_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
-                                       const double* HR, const double* HRv, const double* Hd, const double* Hdv,
-                                       const double* Hld, const double* Hrd, int npts, const double* E,
-                                       const int* qidx, const int* zero_flag, double eta, double eta0,
-                                       double dev_factor, double convergence, int max_iter, double lambda_eta,
-                                       double a_z_l, double a_z_r, int nshift, int stride_l, int nrep_l,
-                                       const double* phase_l, int stride_r, int nrep_r, const double* phase_r,
-                                       double* transl, double* transr, double* mode_sums, int* status, int* nprop,
-                                       double* mode_kz, int* mode_bz, double* col_sums, void* work,
-                                       size_t work_bytes, void* stream) {
+int pf_transport_tdb_modes_ex_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
+                                  const double* HR, const double* HRv, const double* Hd, const double* Hdv,
+                                  const double* Hld, const double* Hrd, int npts, const double* E,
+                                  const int* qidx, const int* zero_flag, double eta, double eta0,
+                                  double dev_factor, double convergence, int max_iter, double lambda_eta,
+                                  double a_z_l, double a_z_r, int nshift, int stride_l, int nrep_l,
+                                  const double* phase_l, int stride_r, int nrep_r, const double* phase_r,
+                                  int flags, double* transl, double* transr, double* mode_sums, int* status,
+                                  int* nprop, double* mode_kz, int* mode_bz, double* col_sums, void* work,
+                                  size_t work_bytes, void* stream) {
+  if (flags & ~PF_MODES_ELECTRON) return set_err(PF_ERR_ARG, "pf_modes: unknown flags");
   if ((mode_kz != nullptr) != (mode_bz != nullptr) || (mode_kz != nullptr) != (col_sums != nullptr))
     return set_err(PF_ERR_ARG, "pf_modes: mode_kz, mode_bz and col_sums are all given or all null");
   if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0)
@@ -660,6 +668,7 @@ int pf_transport_tdb_modes_permode_dev(int n, int nl, int nr, int L, int nq, con
     P.lead_mirror = mirror;
   }
   ModeGeom geo;
+  geo.electron = (flags & PF_MODES_ELECTRON) != 0;
   geo.lambda_eta = lambda_eta;
   geo.a_z_l = a_z_l;
   geo.a_z_r = a_z_r;
@@ -686,6 +695,23 @@ int pf_transport_tdb_modes_permode_dev(int n, int nl, int nr, int L, int nq, con
     MD_CUDA(cudaGetLastError());
   }
   return PF_SUCCESS;
+}
+
+int pf_transport_tdb_modes_permode_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
+                                       const double* HR, const double* HRv, const double* Hd, const double* Hdv,
+                                       const double* Hld, const double* Hrd, int npts, const double* E,
+                                       const int* qidx, const int* zero_flag, double eta, double eta0,
+                                       double dev_factor, double convergence, int max_iter, double lambda_eta,
+                                       double a_z_l, double a_z_r, int nshift, int stride_l, int nrep_l,
+                                       const double* phase_l, int stride_r, int nrep_r, const double* phase_r,
+                                       double* transl, double* transr, double* mode_sums, int* status, int* nprop,
+                                       double* mode_kz, int* mode_bz, double* col_sums, void* work,
+                                       size_t work_bytes, void* stream) {
+  return pf_transport_tdb_modes_ex_dev(n, nl, nr, L, nq, HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd, npts, E, qidx,
+                                       zero_flag, eta, eta0, dev_factor, convergence, max_iter, lambda_eta, a_z_l,
+                                       a_z_r, nshift, stride_l, nrep_l, phase_l, stride_r, nrep_r, phase_r, 0,
+                                       transl, transr, mode_sums, status, nprop, mode_kz, mode_bz, col_sums, work,
+                                       work_bytes, stream);
 }
 
 int pf_transport_tdb_modes_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,

@@ -1025,28 +1025,10 @@ bool make_plan(int n, int nl, int nr, int L, int nq, int npts, MixedPlan& P) {
   return true;
 }
 
-// Points per chunk of the two-stream schedule: with FP64 leads the
-// decimations (FP64 pipe) of one chunk run while the FP32 factorisation and
-// refinement of the previous chunk run on the other stream.
-int chunk_count(bool warp_engine, int npts, int lead_fp64) {
-  if (!lead_fp64 || !warp_engine) return 1;
-  return npts >= 512 ? 4 : (npts >= 256 ? 2 : 1);
-}
-
-// Bytes for either lead arithmetic: one plan over all points (df64 leads),
-// or two regions of a chunk plan used alternately by the two streams.
 size_t mixed_workspace_bytes(int n, int nl, int nr, int L, int nq, int npts) {
   MixedPlan P;
   if (!make_plan(n, nl, nr, L, nq, npts, P)) return 0;
-  size_t total = P.total;
-  const int nch = chunk_count(P.warp_engine, npts, 1);
-  if (nch > 1) {
-    MixedPlan C;
-    if (!make_plan(n, nl, nr, L, nq, (npts + nch - 1) / nch, C)) return 0;
-    const size_t two = 2 * al256(C.total);
-    if (two > total) total = two;
-  }
-  return total;
+  return P.total;
 }
 
 // ===========================================================================
@@ -1327,7 +1309,7 @@ namespace {
 int mixed_launch(const MixedPlan& plan, int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
                  const double* HR, const double* HRv, const double* Hd, const double* Hdv, const double* Hld,
                  const double* Hrd, int npts, const double* E, const int* qidx, const int* zero_flag, double eta,
-                 double eta0, double dev_factor, double convergence, int max_iter, int refine_iters, int lead_fp64,
+                 double eta0, double dev_factor, double convergence, int max_iter, int refine_iters, int lead_mode,
                  double* transl, int* status, int* iters, void* work, cudaStream_t st) {
   const MixedLayout& lay = plan.lay;
   const int S = (lay.base.m + 31) / 32;
@@ -1401,7 +1383,7 @@ int mixed_launch(const MixedPlan& plan, int n, int nl, int nr, int L, int nq, co
   sys.dHLv = reinterpret_cast<const cx<double>*>(HLv);
   sys.dHR = reinterpret_cast<const cx<double>*>(HR);
   sys.dHRv = reinterpret_cast<const cx<double>*>(HRv);
-  sys.lead_fp64 = lead_fp64;
+  sys.lead_mode = lead_mode;
   sys.fHR = ff[2];
   sys.fHd = ff[4];
   sys.fHdv = ff[5];
@@ -1493,19 +1475,6 @@ int mixed_launch(const MixedPlan& plan, int n, int nl, int nr, int L, int nq, co
   return PF_SUCCESS;
 }
 
-std::mutex g_aux_mu;
-cudaStream_t g_aux_stream[128] = {};
-
-int aux_stream(cudaStream_t* out) {
-  int dev = 0;
-  PF_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 128) return set_err(PF_ERR_ARG, "pf: device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_aux_mu);
-  if (!g_aux_stream[dev]) PF_CUDA(cudaStreamCreateWithFlags(&g_aux_stream[dev], cudaStreamNonBlocking));
-  *out = g_aux_stream[dev];
-  return PF_SUCCESS;
-}
-
 int mixed_ex(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv, const double* HR,
              const double* HRv, const double* Hd, const double* Hdv, const double* Hld, const double* Hrd, int npts,
              const double* E, const int* qidx, const int* zero_flag, double eta, double eta0, double dev_factor,
@@ -1518,54 +1487,19 @@ int mixed_ex(int n, int nl, int nr, int L, int nq, const double* HL, const doubl
     return set_err(PF_ERR_ARG, "pf: null block pointer");
   if (max_iter <= 0 || refine_iters < 0 || refine_iters > 16)
     return set_err(PF_ERR_ARG, "pf: max_iter must be positive and refine_iters in [0, 16]");
-  if (lead_arith != PF_ARITH_FP64 && lead_arith != PF_ARITH_DF64)
-    return set_err(PF_ERR_ARG, "pf: lead_arith must be PF_ARITH_FP64 or PF_ARITH_DF64");
+  if (lead_arith != PF_ARITH_FP64 && lead_arith != PF_ARITH_DF64 && lead_arith != PF_ARITH_SPLIT)
+    return set_err(PF_ERR_ARG, "pf: lead_arith must be PF_ARITH_FP64, PF_ARITH_DF64 or PF_ARITH_SPLIT");
   if (npts == 0) return PF_SUCCESS;
-  const int lead_fp64 = lead_arith == PF_ARITH_FP64;
+  const int lead_mode = lead_arith == PF_ARITH_FP64 ? pf::PF_LEAD_FP64
+                                                    : (lead_arith == PF_ARITH_DF64 ? pf::PF_LEAD_DF64 : pf::PF_LEAD_SPLIT);
   MixedPlan plan;
   if (!make_plan(n, nl, nr, L, nq, npts, plan)) return set_err(PF_ERR_SIZE, "pf: kernel does not fit on the device");
   DevInfo d = device_info();
   if (plan.lay.smem > d.smem_optin) return set_err(PF_ERR_SIZE, "pf: working set exceeds shared memory");
-  cudaStream_t st = (cudaStream_t)stream;
-  const int nch = chunk_count(plan.warp_engine, npts, lead_fp64);
-  if (nch == 1) {
-    if (!work || work_bytes < plan.total) return set_err(PF_ERR_ARG, "pf: workspace too small");
-    return mixed_launch(plan, n, nl, nr, L, nq, HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd, npts, E, qidx, zero_flag, eta,
-                        eta0, dev_factor, convergence, max_iter, refine_iters, lead_fp64, transl, status, iters,
-                        work, st);
-  }
-  const int cs = (npts + nch - 1) / nch;
-  MixedPlan pc;
-  if (!make_plan(n, nl, nr, L, nq, cs, pc)) return set_err(PF_ERR_SIZE, "pf: kernel does not fit on the device");
-  const size_t region = al256(pc.total);
-  if (!work || work_bytes < 2 * region) return set_err(PF_ERR_ARG, "pf: workspace too small");
-  cudaStream_t aux = nullptr;
-  rc = aux_stream(&aux);
-  if (rc != PF_SUCCESS) return rc;
-  cudaEvent_t fork = nullptr, join = nullptr;
-  PF_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
-  PF_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
-  PF_CUDA(cudaEventRecord(fork, st));
-  PF_CUDA(cudaStreamWaitEvent(aux, fork, 0));
-  for (int c = 0; c < nch && rc == PF_SUCCESS; ++c) {
-    const int p0 = c * cs;
-    const int cnt = npts - p0 < cs ? npts - p0 : cs;
-    if (cnt <= 0) break;
-    char* wr = reinterpret_cast<char*>(work) + (size_t)(c & 1) * region;
-    rc = mixed_launch(pc, n, nl, nr, L, nq, HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd, cnt, E + p0,
-                      qidx ? qidx + p0 : nullptr, zero_flag ? zero_flag + p0 : nullptr, eta, eta0, dev_factor,
-                      convergence, max_iter, refine_iters, lead_fp64, transl + p0, status + p0,
-                      iters ? iters + 2 * (size_t)p0 : nullptr, wr, (c & 1) ? aux : st);
-  }
-  // the caller's stream waits for the other stream's chunks (also on error,
-  // so that nothing is left running behind the caller's back)
-  cudaError_t e1 = cudaEventRecord(join, aux);
-  cudaError_t e2 = e1 == cudaSuccess ? cudaStreamWaitEvent(st, join, 0) : e1;
-  cudaEventDestroy(fork);
-  cudaEventDestroy(join);
-  if (rc != PF_SUCCESS) return rc;
-  if (e2 != cudaSuccess) return cuda_err(e2, "pf: joining the second stream");
-  return PF_SUCCESS;
+  if (!work || work_bytes < plan.total) return set_err(PF_ERR_ARG, "pf: workspace too small");
+  return mixed_launch(plan, n, nl, nr, L, nq, HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd, npts, E, qidx, zero_flag, eta,
+                      eta0, dev_factor, convergence, max_iter, refine_iters, lead_mode, transl, status, iters, work,
+                      (cudaStream_t)stream);
 }
 }  // namespace
 

@@ -168,21 +168,29 @@ __device__ __forceinline__ int exp_of_maxbits(unsigned long long m) {
   return ef == 0 ? -1022 : ef - 1022;
 }
 
-// one thread per vector (consecutive vectors adjacent in memory)
+// 32 vectors per block, 8 threads along each (consecutive vectors adjacent
+// in memory: a warp reads 32 neighbouring elements per step)
 __global__ void vec_exp_thread(VecSet V, const int* active, int* e) {
   const int b = blockIdx.y;
   if (active && !active[b]) return;
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= V.nvec) return;
-  const double2* p = V.base + (size_t)b * V.sb + (size_t)v * V.sv;
+  __shared__ unsigned long long red[8][32];
+  const int v = blockIdx.x * 32 + threadIdx.x;
   unsigned long long m = 0;
-  for (int j = 0; j < V.len; ++j) {
-    const double2 a = p[(size_t)j * V.sj];
-    const unsigned long long x = mag_bits(a.x), y = mag_bits(a.y);
-    m = x > m ? x : m;
-    m = y > m ? y : m;
+  if (v < V.nvec) {
+    const double2* p = V.base + (size_t)b * V.sb + (size_t)v * V.sv;
+    for (int j = threadIdx.y; j < V.len; j += 8) {
+      const double2 a = p[(size_t)j * V.sj];
+      const unsigned long long x = mag_bits(a.x), y = mag_bits(a.y);
+      m = x > m ? x : m;
+      m = y > m ? y : m;
+    }
   }
-  e[(size_t)b * V.nvec + v] = exp_of_maxbits(m);
+  red[threadIdx.y][threadIdx.x] = m;
+  __syncthreads();
+  if (threadIdx.y == 0 && v < V.nvec) {
+    for (int k = 1; k < 8; ++k) m = red[k][threadIdx.x] > m ? red[k][threadIdx.x] : m;
+    e[(size_t)b * V.nvec + v] = exp_of_maxbits(m);
+  }
 }
 // one warp per vector (contiguous vectors)
 __global__ void vec_exp_warp(VecSet V, const int* active, int* e) {
@@ -444,12 +452,254 @@ __global__ void __launch_bounds__(kThreads, 2)
 }
 
 // ---------------------------------------------------------------------------
+// Pipelined product kernel: the same tile and arithmetic as tc_prod_kernel,
+// with warp roles and double buffering so that loads, products and drains
+// overlap.  192 threads: warp 0 issues the TMA loads, warp 1 the tcgen05.mma
+// (one elected lane each), warps 2..5 drain TMEM (warp w reads lanes
+// 32 (w mod 4) .. +31) and write C.  Shared memory: two A chunks (128 rows x
+// 256 K) and two B chunks (64 rows x 256 K); TMEM: two accumulators for the
+// exact pairs (drained while the next pair accumulates) and the low slot.
+// Job order, identical in every role: chunk c, slice s of A, slice t of B.
+// Every wait is bounded and also gives up when another role has given up.
+// ---------------------------------------------------------------------------
+constexpr int kPipeThreads = 192;
+constexpr int kPipeTmemCols = 256;   // top slots [0, 64), [64, 128); low [128, 192)
+constexpr int kPipeSmem = 1024 + 2 * kSmemA + 2 * kSmemB + 256;
+static_assert(3 * kBN <= kPipeTmemCols, "TMEM slots");
+
+enum { BA_FULL = 0, BA_EMPTY = 2, BB_FULL = 4, BB_EMPTY = 6, BACC_FULL = 8, BACC_EMPTY = 10, BLOW = 12, BFIN = 13,
+       NBAR = 14 };
+
+// Bounded wait that also returns false once *abort is set; a wait that runs
+// out of time sets *abort itself.
+__device__ __forceinline__ bool mbar_wait_ab(uint32_t bar, uint32_t parity, volatile int* abort) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (*abort) return false;
+    if (clock64() - t0 > kWaitCycles) {
+      *abort = 1;
+      return false;
+    }
+  }
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__global__ void __launch_bounds__(kPipeThreads, 1)
+    tc_prod_pipe_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, ProdArgs p) {
+  const int b = blockIdx.z;
+  if (p.active && !p.active[b]) return;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                         ~(uintptr_t)1023);
+  unsigned char* sA = smem;                   // 2 stages of kSmemA
+  unsigned char* sB = smem + 2 * kSmemA;      // 2 stages of kSmemB
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sB + 2 * kSmemB);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + NBAR);
+  volatile int* abort = reinterpret_cast<volatile int*>(tmem_holder + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
+  const int ba = p.a_shared ? 0 : b, bb = p.b_shared ? 0 : b;
+  auto bar = [&](int i) { return smem_u32(&bars[i]); };
+
+  if (tid == 0) {
+    for (int i = 0; i < NBAR; ++i) mbar_init(bar(i), (i == BACC_EMPTY || i == BACC_EMPTY + 1) ? 4u : 1u);
+    *abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
+                 "r"(kPipeTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+  const int nchunk = (p.kp + kChunk - 1) / kChunk;
+
+  if (warp == 0) {
+    // ---- TMA producer
+    if (lane == 0) {
+      int ja = 0, jb = 0;
+      uint32_t last_a = 0, last_a_ph = 0, last_b = 0, last_b_ph = 0;
+      bool ok = true;
+      for (int c = 0; c < nchunk && ok; ++c) {
+        const int k0 = c * kChunk;
+        const int ks = min(kBoxes, (p.kp - k0) / kKStep);
+        for (int s = 0; s < kSlices && ok; ++s) {
+          const int as = ja & 1, ka = ja >> 1;
+          if (!(ok = mbar_wait_ab(bar(BA_EMPTY + as), (ka & 1) ^ 1, abort))) break;
+          mbar_expect_tx(bar(BA_FULL + as), (uint32_t)(ks * kBoxA));
+          for (int u = 0; u < ks; ++u)
+            tma_load_4d(smem_u32(sA + as * kSmemA + u * kBoxA), &ta, k0 + u * kKStep, m0, s, ba, bar(BA_FULL + as));
+          last_a = bar(BA_FULL + as);
+          last_a_ph = ka & 1;
+          ++ja;
+          for (int t = 0; s + t <= kSlices - 1; ++t) {
+            const int bs = jb & 1, kb = jb >> 1;
+            if (!(ok = mbar_wait_ab(bar(BB_EMPTY + bs), (kb & 1) ^ 1, abort))) break;
+            mbar_expect_tx(bar(BB_FULL + bs), (uint32_t)(ks * kBoxB));
+            for (int u = 0; u < ks; ++u)
+              tma_load_4d(smem_u32(sB + bs * kSmemB + u * kBoxB), &tb, k0 + u * kKStep, n0, t, bb,
+                          bar(BB_FULL + bs));
+            last_b = bar(BB_FULL + bs);
+            last_b_ph = kb & 1;
+            ++jb;
+          }
+        }
+      }
+      if (!ok) {
+        // copies still in flight land before the CTA's shared memory is released
+        if (last_a) (void)mbar_wait(last_a, last_a_ph);
+        if (last_b) (void)mbar_wait(last_b, last_b_ph);
+      }
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16(kBM, kBN);
+      int ja = 0, jb = 0, jt = 0;
+      bool low_init = false, ok = true;
+      for (int c = 0; c < nchunk && ok; ++c) {
+        const int k0 = c * kChunk;
+        const int ks = min(kBoxes, (p.kp - k0) / kKStep);
+        for (int s = 0; s < kSlices && ok; ++s) {
+          const int as = ja & 1, ka = ja >> 1;
+          if (!(ok = mbar_wait_ab(bar(BA_FULL + as), ka & 1, abort))) break;
+          for (int t = 0; s + t <= kSlices - 1; ++t) {
+            const int d = s + t + 2;
+            const bool top = d <= kTopD;
+            const int bs = jb & 1, kb = jb >> 1;
+            if (!(ok = mbar_wait_ab(bar(BB_FULL + bs), kb & 1, abort))) break;
+            const int slot = jt & 1, kt = jt >> 1;
+            if (top && !(ok = mbar_wait_ab(bar(BACC_EMPTY + slot), (kt & 1) ^ 1, abort))) break;
+            tc_fence_after();
+            const uint32_t dcol = top ? (uint32_t)(slot * kBN) : (uint32_t)(2 * kBN);
+            for (int u = 0; u < ks; ++u) {
+#pragma unroll
+              for (int kk = 0; kk < kKStep / 16; ++kk) {
+                const uint64_t ad = desc_sw128(smem_u32(sA + as * kSmemA + u * kBoxA + kk * 32));
+                const uint64_t bd = desc_sw128(smem_u32(sB + bs * kSmemB + u * kBoxB + kk * 32));
+                const uint32_t acc = top ? (uint32_t)((u | kk) != 0) : (uint32_t)(low_init || (u | kk) != 0);
+                mma_bf16(tmem + dcol, ad, bd, idesc, acc);
+              }
+            }
+            if (!top) low_init = true;
+            mma_commit(bar(BB_EMPTY + bs));
+            if (top) {
+              mma_commit(bar(BACC_FULL + slot));
+              ++jt;
+            }
+            if (s + t == kSlices - 1) mma_commit(bar(BA_EMPTY + as));
+            ++jb;
+          }
+          ++ja;
+        }
+      }
+      if (ok) mma_commit(bar(BLOW));
+      mma_commit(bar(BFIN));  // arrives once every product issued here has completed
+    }
+  } else {
+    // ---- epilogue: drains of the exact pairs, then the output tile
+    const int sub = warp & 3;  // TMEM lane quarter of this warp
+    const uint32_t lane_base = tmem + ((uint32_t)(sub * 32) << 16);
+    long long F[kBN];
+#pragma unroll
+    for (int j = 0; j < kBN; ++j) F[j] = 0;
+    int jt = 0;
+    bool ok = true;
+    for (int c = 0; c < nchunk && ok; ++c) {
+      for (int s = 0; s < kSlices && ok; ++s) {
+        for (int t = 0; s + t <= kSlices - 1 && ok; ++t) {
+          const int d = s + t + 2;
+          if (d > kTopD) continue;
+          const int slot = jt & 1, kt = jt >> 1;
+          ok = __all_sync(0xffffffffu, mbar_wait_ab(bar(BACC_FULL + slot), kt & 1, abort));
+          if (!ok) break;
+          tc_fence_after();
+          const float scale = __int_as_float((127 + kBeta * d) << 23);
+          const int sh = kBeta * (kTopD - d);
+#pragma unroll
+          for (int q = 0; q < kBN / 16; ++q) {
+            uint32_t r[16];
+            tmem_ld16(lane_base + slot * kBN + q * 16, r);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const float f = fmaf(__uint_as_float(r[j]), scale, 12582912.0f);
+              const int I = __float_as_int(f) - 0x4B400000;
+              F[q * 16 + j] += (long long)I << sh;
+            }
+          }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(bar(BACC_EMPTY + slot));
+          ++jt;
+        }
+      }
+    }
+    if (ok) ok = mbar_wait_ab(bar(BLOW), 0, abort);
+    ok = __all_sync(0xffffffffu, ok);
+    if (ok) {
+      tc_fence_after();
+      const int R = m0 + sub * 32 + lane;
+      const bool rowok = R < 2 * p.m;
+      const int i = R >> 1, part = R & 1;
+      const int ea = rowok ? p.ea[(size_t)ba * p.m + i] : 0;
+      double* Cb = p.C + (size_t)b * p.sC * 2;
+#pragma unroll
+      for (int q = 0; q < kBN / 16; ++q) {
+        uint32_t r[16];
+        tmem_ld16(lane_base + 2 * kBN + q * 16, r);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int col = n0 + q * 16 + j;
+          if (!rowok || col >= p.n) continue;
+          const int eb = p.eb[(size_t)bb * p.n + col];
+          double v;
+          if (ea == kExpBad || eb == kExpBad) {
+            v = __longlong_as_double(0x7FF8000000000000ll);
+          } else {
+            const double top = (double)F[q * 16 + j] * 0x1p-42;  // LSB 2^(-7 kTopD)
+            v = scalbn(top + (double)__uint_as_float(r[j]), ea + eb);
+          }
+          v *= p.alpha;
+          const size_t at = 2 * ((size_t)i + (size_t)col * p.ldc) + part;
+          if (p.beta != 0.0) v = fma(p.beta, Cb[at], v);
+          if (p.H) v -= p.H[(size_t)b * p.sH * 2 + 2 * ((size_t)i + (size_t)col * p.ldh) + part];
+          if (p.zdiag && i == col) v += part ? p.zdiag[b].y : p.zdiag[b].x;
+          Cb[at] = v;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // every product has completed before TMEM is released
+  (void)mbar_wait(bar(BFIN), 0);
+  if (tid == 0 && *abort && p.err) atomicOr(p.err, 1);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kPipeTmemCols));
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 EncodeTiledFn g_encode = nullptr;
+bool g_pipe = true;  // pipelined product kernel (false: the synchronous one)
 std::once_flag g_encode_once;
 
 void load_encode() {
@@ -507,7 +757,7 @@ Carve carve(char* base, int m, int n, int k, int nba, int nbb) {
 
 void launch_exp(const VecSet& V, const int* active, int* e, cudaStream_t st) {
   if (V.sv == 1)
-    vec_exp_thread<<<dim3((V.nvec + 127) / 128, V.nbatch), 128, 0, st>>>(V, active, e);
+    vec_exp_thread<<<dim3((V.nvec + 31) / 32, V.nbatch), dim3(32, 8), 0, st>>>(V, active, e);
   else
     vec_exp_warp<<<dim3((V.nvec + 7) / 8, V.nbatch), 256, 0, st>>>(V, active, e);
 }
@@ -576,10 +826,16 @@ cudaError_t zgemm(const ZgemmArgs& g, void* work, size_t work_bytes, int* err, c
   p.ldh = g.ldh;
   p.sH = g.sH;
   p.err = err;
-  e = cudaFuncSetAttribute(tc_prod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-  if (e != cudaSuccess) return e;
   const dim3 grid((2 * g.m + kBM - 1) / kBM, (g.n + kBN - 1) / kBN, g.batch);
-  tc_prod_kernel<<<grid, kThreads, kSmemBytes, st>>>(ta, tb, p);
+  if (g_pipe) {
+    e = cudaFuncSetAttribute(tc_prod_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPipeSmem);
+    if (e != cudaSuccess) return e;
+    tc_prod_pipe_kernel<<<grid, kPipeThreads, kPipeSmem, st>>>(ta, tb, p);
+  } else {
+    e = cudaFuncSetAttribute(tc_prod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if (e != cudaSuccess) return e;
+    tc_prod_kernel<<<grid, kThreads, kSmemBytes, st>>>(ta, tb, p);
+  }
   return cudaGetLastError();
 }
 

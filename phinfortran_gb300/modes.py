@@ -137,7 +137,8 @@ class LeadGeometry:
 
 
 def transport_tdb_modes(E, blocks, geometry, ksc, *, eta, eta0, convergence, lambda_eta, a_z_l, a_z_r,
-                        dev_factor=10.0, qidx=None, zero_flag=None, max_iter=1000, check=True, per_mode=False):
+                        dev_factor=10.0, qidx=None, zero_flag=None, max_iter=1000, check=True, per_mode=False,
+                        electron=False):
     """Transmission and its mode-resolved split for a batch of points.
 
     ``blocks``: one q (dict) or a TdbBlocks stack; ``ksc``: (nq, 3)
@@ -146,6 +147,9 @@ def transport_tdb_modes(E, blocks, geometry, ksc, *, eta, eta0, convergence, lam
     and status; with ``per_mode`` also mode_kz, mode_bz (npts, 4, mm) and
     col_sums (npts, 4, mm, nshift) of pf_transport_tdb_modes_permode_dev
     (problems adv-L, ret-L, ret-R, adv-R; matrices tlr, trl, rrr, rll).
+    ``electron`` selects the tight-binding normalisation (velocity matrices
+    and t / r without the phonon a_z / (2 sqrt(E)) factors; energies may be
+    negative).
     """
     import torch
     lib = _abi.load()
@@ -175,19 +179,21 @@ def transport_tdb_modes(E, blocks, geometry, ksc, *, eta, eta0, convergence, lam
         raise _abi.PFError(-3, "mode-resolved kernel does not fit (block size > 48?)")
     work = torch.empty(ws, dtype=torch.uint8, device="cuda")
     p = lambda t: None if t is None else t.data_ptr()
-    args = (n, nl, nr, L, nq, *[dev[k].data_ptr() for k in BLOCK_NAMES], npts, Ed.data_ptr(), p(qd), p(zd), eta,
+    head = (n, nl, nr, L, nq, *[dev[k].data_ptr() for k in BLOCK_NAMES], npts, Ed.data_ptr(), p(qd), p(zd), eta,
             eta0, dev_factor, convergence, max_iter, lambda_eta, a_z_l, a_z_r, geometry.nshift, sl, rl_,
-            ph_l.data_ptr(), sr, rr_, ph_r.data_ptr(), tl.data_ptr(), tr.data_ptr(), sums.data_ptr(), st.data_ptr(),
-            npr.data_ptr())
+            ph_l.data_ptr(), sr, rr_, ph_r.data_ptr())
+    outs = (tl.data_ptr(), tr.data_ptr(), sums.data_ptr(), st.data_ptr(), npr.data_ptr())
     tail = (work.data_ptr(), ws, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    flags = 1 if electron else 0   # PF_MODES_ELECTRON
     if per_mode:
         mm = max(nl, nr)
         kz = torch.zeros((max(npts, 1), 4, mm), dtype=torch.float64, device="cuda")
         bz = torch.zeros((max(npts, 1), 4, mm), dtype=torch.int32, device="cuda")
         cs = torch.zeros((max(npts, 1), 4, mm, geometry.nshift), dtype=torch.float64, device="cuda")
-        rc = lib.pf_transport_tdb_modes_permode_dev(*args, kz.data_ptr(), bz.data_ptr(), cs.data_ptr(), *tail)
+        rc = lib.pf_transport_tdb_modes_ex_dev(*head, flags, *outs, kz.data_ptr(), bz.data_ptr(), cs.data_ptr(),
+                                               *tail)
     else:
-        rc = lib.pf_transport_tdb_modes_dev(*args, *tail)
+        rc = lib.pf_transport_tdb_modes_ex_dev(*head, flags, *outs, None, None, None, *tail)
     if rc != 0:
         raise _abi.PFError(rc, lib.pf_modes_last_error().decode(errors="replace"))
     torch.cuda.synchronize()

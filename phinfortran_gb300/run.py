@@ -54,7 +54,7 @@ def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("workload", choices=["ribbon", "ribbon3", "sc", "diamond", "sisi"])
     ap.add_argument("--mode", default="transport", choices=["transport", "modes", "grad"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "tc", "df64"])
     ap.add_argument("--arith", default="df64", choices=["fp64", "df64"], help="adjoint arithmetic")
     ap.add_argument("--ckpt", type=int, default=0, help="adjoint checkpoint interval (0: sqrt(L+2))")
     ap.add_argument("--energies", type=int, default=16)

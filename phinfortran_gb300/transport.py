@@ -222,9 +222,12 @@ class DeviceTransport:
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.precision = precision
         self.refine_iters = int(refine_iters)
-        if lead_arith not in ("fp64", "df64"):
-            raise ValueError("lead_arith must be 'fp64' or 'df64'")
-        self.lead_arith = 0 if lead_arith == "fp64" else 1   # PF_ARITH_FP64 / PF_ARITH_DF64
+        # lead decimations of the mixed path: PF_ARITH_FP64 (default),
+        # PF_ARITH_SPLIT (first steps FP64, the rest double-float) or PF_ARITH_DF64
+        lead_codes = {"split": 3, "fp64": 0, "df64": 1}
+        if lead_arith not in lead_codes:
+            raise ValueError("lead_arith must be 'split', 'fp64' or 'df64'")
+        self.lead_arith = lead_codes[lead_arith]
         if precision == "mixed":
             want_transr = False
         self.params = (eta, eta0, dev_factor, convergence, max_iter, int(bool(want_transr)))
