@@ -340,6 +340,7 @@ enum : int {
   PF_SINGULAR = 1,       // exact zero pivot (reference: ZGETRF info > 0, util.f90:44-58)
   PF_NAN = 2,            // non-finite entry (reference: ifnan stop, util.f90:29-32)
   PF_NOT_CONVERGED = 4,  // decimation hit its iteration cap
+  PF_TC_TIMEOUT = 16,    // a tensor-core product's completion wait gave up (result not used)
 };
 
 // In-place inverse with explicit row exchanges (pivot rows swapped into

@@ -21,6 +21,7 @@
 //      correction by the stored FP32 factors, X += dX in df64;
 //   5. Caroli trace in df64.
 #pragma once
+#include "tc_small.cuh"
 #include "transport.cuh"
 
 namespace pf {
@@ -188,9 +189,58 @@ __device__ void copy_cvt(cx<A>* dst, int ldd, bool conj_t, const cx<B>* src, int
 // takes FP64 decimations.  The CTA's df64-sized slots hold the FP64
 // matrices (both 16 bytes per complex element).
 // ---------------------------------------------------------------------------
+// The FP64 decimation (negf/surface.f90:479-497) with its six block
+// products per step on the tensor cores (FP64-grade slice products, see
+// tc_small.cuh) and the inverse in FP64 on the CTA.  On return SM2 holds
+// g = inv(z - es) and G_ES holds es (FP64), as after decimate<double>.
+template <int S>
+__device__ int decimate_tc(const Ctx<double>& c, tc::SmallTC& t, int m, cx<double> z, Op<double> h00,
+                           Op<double> a0, Op<double> b0, double conv, int max_iter, int* iters_out) {
+  const int ld = c.ld;
+  cx<double>* al = c.sm[0];
+  cx<double>* be = c.sm[1];
+  cx<double>* W1 = c.sm[2];
+  cx<double>* e1 = c.gs[G_E1];
+  cx<double>* es = c.gs[G_ES];
+  cx<double>* W2 = c.gs[G_W2];
+  cx<double>* W3 = c.gs[G_W3];
+  int st = PF_OK;
+  copy_in(e1, ld, h00, m, m);
+  copy_in(es, ld, h00, m, m);
+  copy_in(al, ld, a0, m, m);
+  copy_in(be, ld, b0, m, m);
+  double maxdiff = max_abs(al, ld, m, m, c.red);
+  int it = 0;
+  while (maxdiff > conv) {
+    if (it >= max_iter) {
+      st |= PF_NOT_CONVERGED;
+      break;
+    }
+    shift_neg(W1, ld, z, e1, ld, m);                                                 // z - e1
+    st |= inverse(W1, ld, m, c.iw);                                                  // ive
+    bool ok = tc::small_zgemm(t, m, opN<double>(al, ld), opN<double>(W1, ld), tc::OutStore{W2, ld});
+    ok = ok && tc::small_zgemm(t, m, opN<double>(be, ld), opN<double>(W1, ld), tc::OutStore{W3, ld});
+    ok = ok && tc::small_zgemm(t, m, opN<double>(W2, ld), opN<double>(be, ld), tc::OutAcc2{e1, es, ld});
+    ok = ok && tc::small_zgemm(t, m, opN<double>(W3, ld), opN<double>(al, ld), tc::OutAcc{e1, ld});
+    ok = ok && tc::small_zgemm(t, m, opN<double>(W2, ld), opN<double>(al, ld), tc::OutStore{al, ld});
+    ok = ok && tc::small_zgemm(t, m, opN<double>(W3, ld), opN<double>(be, ld), tc::OutStore{be, ld});
+    if (!ok) {
+      st |= PF_TC_TIMEOUT;
+      break;
+    }
+    maxdiff = max_abs(al, ld, m, m, c.red);
+    ++it;
+  }
+  if (maxdiff != maxdiff) st |= PF_NAN;
+  shift_neg(W1, ld, z, es, ld, m);
+  st |= inverse(W1, ld, m, c.iw);
+  if (iters_out) *iters_out = it;
+  return st;
+}
+
 template <int S>
 __device__ int mixed_leads64(const MCtx& mc, const MSys& sys, int q, double E, const Params& P, int* it_l,
-                             int* it_r) {
+                             int* it_r, tc::SmallTC* tcx = nullptr) {
   Ctx<double> c;
   for (int i = 0; i < NSM; ++i) c.sm[i] = reinterpret_cast<cx<double>*>(mc.sm[i]);
   c.gs[G_E1] = reinterpret_cast<cx<double>*>(mc.gs[M_E1]);
@@ -210,8 +260,12 @@ __device__ int mixed_leads64(const MCtx& mc, const MSys& sys, int q, double E, c
   {
     const cx<double>* HL = sys.dHL + (size_t)q * nl * nl;
     const cx<double>* HLv = sys.dHLv + (size_t)q * nl * nl;
-    st |= decimate<double, S>(c, nl, mk<double>(E, -eps), opN<double>(HL, nl), opC<double>(HLv, nl),
-                              opN<double>(HLv, nl), P.convergence, P.max_iter, it_l);
+    if (tcx)
+      st |= decimate_tc<S>(c, *tcx, nl, mk<double>(E, -eps), opN<double>(HL, nl), opC<double>(HLv, nl),
+                           opN<double>(HLv, nl), P.convergence, P.max_iter, it_l);
+    else
+      st |= decimate<double, S>(c, nl, mk<double>(E, -eps), opN<double>(HL, nl), opC<double>(HLv, nl),
+                                opN<double>(HLv, nl), P.convergence, P.max_iter, it_l);
     copy_cvt<float, double>(mc.lu, ld, true, c.sm[2], ld, nl, nl);             // g_0 = g_adv^H
     copy_cvt<df64, double>(mc.gs[M_ESL], ld, true, c.gs[G_ES], ld, nl, nl);    // es_adv^H
     lead_sigma<double, S>(c, nl, HLv);                                         // SM1 = sl_adv
@@ -226,8 +280,12 @@ __device__ int mixed_leads64(const MCtx& mc, const MSys& sys, int q, double E, c
   } else {
     const cx<double>* HR = sys.dHR + (size_t)q * nr * nr;
     const cx<double>* HRv = sys.dHRv + (size_t)q * nr * nr;
-    st |= decimate<double, S>(c, nr, mk<double>(E, eps), opN<double>(HR, nr), opC<double>(HRv, nr),
-                              opN<double>(HRv, nr), P.convergence, P.max_iter, it_r);
+    if (tcx)
+      st |= decimate_tc<S>(c, *tcx, nr, mk<double>(E, eps), opN<double>(HR, nr), opC<double>(HRv, nr),
+                           opN<double>(HRv, nr), P.convergence, P.max_iter, it_r);
+    else
+      st |= decimate<double, S>(c, nr, mk<double>(E, eps), opN<double>(HR, nr), opC<double>(HRv, nr),
+                                opN<double>(HRv, nr), P.convergence, P.max_iter, it_r);
     lead_sigma<double, S>(c, nr, HRv);                                         // SM1 = sr_ret
     copy_cvt<df64, double>(mc.gs[M_SR], ld, false, c.sm[1], ld, nr, nr);
     copy_cvt<float, double>(mc.fsr, ld, false, c.sm[1], ld, nr, nr);
@@ -332,8 +390,8 @@ __device__ int decimate_split(const Ctx<df64>& cd, int m, double E, double eps_s
 // ---------------------------------------------------------------------------
 template <int S>
 __device__ int mixed_leads(const MCtx& mc, const MSys& sys, int q, double E, const Params& P, int* it_l,
-                           int* it_r) {
-  if (sys.lead_mode == PF_LEAD_FP64) return mixed_leads64<S>(mc, sys, q, E, P, it_l, it_r);
+                           int* it_r, tc::SmallTC* tcx = nullptr) {
+  if (sys.lead_mode == PF_LEAD_FP64) return mixed_leads64<S>(mc, sys, q, E, P, it_l, it_r, tcx);
   const bool split = sys.lead_mode == PF_LEAD_SPLIT;
   Ctx<df64> c;
   for (int i = 0; i < NSM; ++i) c.sm[i] = mc.sm[i];

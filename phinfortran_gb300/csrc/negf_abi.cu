@@ -510,6 +510,78 @@ __global__ void __launch_bounds__(kThreads) leads_kernel(pf::MSys sys, pf::Point
 }
 
 
+// Leads kernel of the FP64 lead arithmetic (blocks up to 32): the same work
+// as leads_kernel<1>, the decimations' block products on the tensor cores
+// (tc_small.cuh).  One CTA per SM: it holds all 512 TMEM columns (the
+// dynamic shared memory requested keeps a second CTA off the SM).
+__global__ void __launch_bounds__(kThreads, 1) leads_tc_kernel(pf::MSys sys, pf::Points pts, pf::Params P,
+                                                         pf::Outputs out, MixedLayout lay, size_t per_cta,
+                                                         char* scratch, pf::wp::LeadOut lo, int* lead_status,
+                                                         int* queue) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int S = 1;
+  pf::MCtx c;
+  const size_t mat = lay.base.mat;
+  dcx* s = reinterpret_cast<dcx*>(smem_raw);
+  for (int i = 0; i < pf::NSM_M; ++i) c.sm[i] = i < pf::NSM ? s + i * mat : nullptr;
+  unsigned char* tail = reinterpret_cast<unsigned char*>(s + pf::NSM * mat);
+  c.red = reinterpret_cast<double*>(tail);
+  c.iwd.rowk = reinterpret_cast<dcx*>(tail + 32 * sizeof(double));
+  c.iwd.colk = c.iwd.rowk + lay.base.m;
+  int* ip = reinterpret_cast<int*>(c.iwd.colk + lay.base.m);
+  c.iwd.perm = ip;
+  c.iwd.flag = ip + lay.base.m;
+  c.iwf.rowk = reinterpret_cast<fcx*>(c.iwd.rowk);
+  c.iwf.colk = reinterpret_cast<fcx*>(c.iwd.colk);
+  c.iwf.perm = c.iwd.perm;
+  c.iwf.flag = c.iwd.flag;
+  char* base = scratch + (size_t)blockIdx.x * per_cta;
+  dcx* g = reinterpret_cast<dcx*>(base);
+  for (int i = 0; i < pf::NGM; ++i) c.gs[i] = g + i * mat;
+  // lu/fsr of the CTA scratch hold g_0 and Sigma_R before they are padded out
+  c.xv = g + pf::NGM * mat;
+  c.lu = reinterpret_cast<fcx*>(c.xv);
+  c.yv = c.lu + mat;
+  c.fsr = c.yv + mat;
+  c.ld = lay.base.ld;
+  c.mat = mat;
+  __shared__ int s_p;
+  __shared__ int s_tc_abort;
+  const size_t B = (size_t)pf::wp::NW * pf::wp::NW;
+  // tensor-core tiles after the decimation slots, 1024-aligned
+  unsigned char* tiles = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + lay.smem_leads + 1023) & ~(uintptr_t)1023);
+  pf::tc::SmallTC tcx;
+  pf::tc::small_init(tcx, tiles, &s_tc_abort);
+  for (;;) {
+    if (threadIdx.x == 0) s_p = atomicAdd(queue, 1);
+    __syncthreads();
+    const int p = s_p;
+    __syncthreads();
+    if (p >= pts.npts) break;
+    const int q = pts.qidx ? pts.qidx[p] : 0;
+    int itl = 0, itr = 0;
+    const int st = pf::mixed_leads<S>(c, sys, q, pts.E[p], P, &itl, &itr, &tcx);
+    pad_store_f(lo.g0 + p * B, c.lu, c.ld, sys.nl, true);
+    pad_store_f(lo.fsr + p * B, c.fsr, c.ld, sys.nr, false);
+    pad_store(lo.esl + p * B, c.gs[pf::M_ESL], c.ld, sys.nl, false);
+    pad_store(lo.sr + p * B, c.gs[pf::M_SR], c.ld, sys.nr, false);
+    pad_store(lo.gml + p * B, c.gs[pf::M_GML], c.ld, sys.nl, false);
+    pad_store(lo.gmr + p * B, c.gs[pf::M_GMR], c.ld, sys.nr, false);
+    if (threadIdx.x == 0) {
+      lead_status[p] = st;
+      if (out.iters) {
+        out.iters[2 * p] = itl;
+        out.iters[2 * p + 1] = itr;
+      }
+    }
+    __syncthreads();
+  }
+  pf::tc::small_release(tcx);
+}
+
+
+
 // Refinement residual r_j = b_j - A X (df64) of every point and every
 // extended layer, written in FP32 into the forward-vector slab (the forward
 // pass consumes r_j before it overwrites the slot with y_j).
@@ -1427,8 +1499,17 @@ int mixed_launch(const MixedPlan& plan, int n, int nl, int nr, int L, int nq, co
     sl.corr = reinterpret_cast<float*>(w + plan.off_refine);
     int* rlist = reinterpret_cast<int*>(sl.corr + np);
     int* rcount = queue + 2;
-    leads_kernel<1><<<plan.grid_a, kThreads, lay.smem_leads, st>>>(sys, pts, P, out, lay, plan.per_cta_a, scratch, lo,
-                                                              lstat, queue);
+    if (lead_mode == pf::PF_LEAD_FP64) {
+      // tensor-core products in the FP64 decimations: one CTA per SM
+      const size_t smem_tc = lay.smem_leads + 1024 + (size_t)pf::tc::kSmallSmem;
+      PF_CUDA(cudaFuncSetAttribute(leads_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tc));
+      const int grid_tc = plan.grid_a < device_info().sms ? plan.grid_a : device_info().sms;
+      leads_tc_kernel<<<grid_tc, kThreads, smem_tc, st>>>(sys, pts, P, out, lay, plan.per_cta_a, scratch, lo, lstat,
+                                                          queue);
+    } else {
+      leads_kernel<1><<<plan.grid_a, kThreads, lay.smem_leads, st>>>(sys, pts, P, out, lay, plan.per_cta_a, scratch,
+                                                                      lo, lstat, queue);
+    }
     PF_CUDA(cudaGetLastError());
     // factorisation + back substitution, then each refinement sweep as a
     // parallel residual kernel followed by the warp-per-point correction,
