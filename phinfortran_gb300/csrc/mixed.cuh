@@ -218,12 +218,16 @@ __device__ int decimate_tc(const Ctx<double>& c, tc::SmallTC& t, int m, cx<doubl
     }
     shift_neg(W1, ld, z, e1, ld, m);                                                 // z - e1
     st |= inverse(W1, ld, m, c.iw);                                                  // ive
-    bool ok = tc::small_zgemm(t, m, opN<double>(al, ld), opN<double>(W1, ld), tc::OutStore{W2, ld});
-    ok = ok && tc::small_zgemm(t, m, opN<double>(be, ld), opN<double>(W1, ld), tc::OutStore{W3, ld});
-    ok = ok && tc::small_zgemm(t, m, opN<double>(W2, ld), opN<double>(be, ld), tc::OutAcc2{e1, es, ld});
-    ok = ok && tc::small_zgemm(t, m, opN<double>(W3, ld), opN<double>(al, ld), tc::OutAcc{e1, ld});
-    ok = ok && tc::small_zgemm(t, m, opN<double>(W2, ld), opN<double>(al, ld), tc::OutStore{al, ld});
-    ok = ok && tc::small_zgemm(t, m, opN<double>(W3, ld), opN<double>(be, ld), tc::OutStore{be, ld});
+    // the six products of a step as three stacked pairs sharing the right operand:
+    //   [A; B] = [alpha; beta] ive,  e1, es += A beta with beta' = B beta,
+    //   alpha' = A alpha with e1 += B alpha
+    using tc::OutPair;
+    bool ok = tc::small_zgemm2(t, m, opN<double>(al, ld), opN<double>(be, ld), opN<double>(W1, ld),
+                               OutPair{{tc::OUT_STORE, tc::OUT_STORE}, {W2, W3}, {nullptr, nullptr}, ld});
+    ok = ok && tc::small_zgemm2(t, m, opN<double>(W2, ld), opN<double>(W3, ld), opN<double>(be, ld),
+                                OutPair{{tc::OUT_ACC2, tc::OUT_STORE}, {e1, be}, {es, nullptr}, ld});
+    ok = ok && tc::small_zgemm2(t, m, opN<double>(W2, ld), opN<double>(W3, ld), opN<double>(al, ld),
+                                OutPair{{tc::OUT_STORE, tc::OUT_ACC}, {al, e1}, {nullptr, nullptr}, ld});
     if (!ok) {
       st |= PF_TC_TIMEOUT;
       break;

@@ -27,7 +27,7 @@ constexpr int kSmallATile = 128 * 128;            // bytes of one A slice tile
 constexpr int kSmallBTile = kSmallN * 128;        // bytes of one B slice tile
 constexpr int kSmallTmemCols = 512;
 constexpr int kSmallLow = 15;                     // TMEM slot of the light pairs
-constexpr int kSmallSmem = 2 * kSmallATile + kSlices * kSmallBTile + 2 * 32 * 4 + 64;
+constexpr int kSmallSmem = 2 * kSmallATile + kSlices * kSmallBTile + 3 * 32 * 4 + 64;
 
 // slot of the exact pair (s, t) (0-based slices, s + t + 2 <= kTopD), in the
 // order d = 2, 3, ..., kTopD; -1 for the light pairs
@@ -41,7 +41,7 @@ static_assert((kTopD - 1) * kTopD / 2 == kSmallLow, "15 exact pairs");
 struct SmallTC {
   unsigned char* a_tile;  // 2 tiles, 1024-aligned
   unsigned char* b_tile;  // kSlices tiles, 1024-aligned
-  int* ea;                // [32] row exponents of op(A)
+  int* ea;                // [64] row exponents of the two stacked op(A)
   int* eb;                // [32] column exponents of op(B)
   uint64_t* bar;          // [2] mbarriers: products reading A tile 0 / 1 done
   uint32_t tmem;          // TMEM base address
@@ -67,7 +67,7 @@ __device__ inline void small_init(SmallTC& t, unsigned char* smem_1024, int* abo
   t.a_tile = smem_1024;
   t.b_tile = smem_1024 + 2 * kSmallATile;
   t.ea = reinterpret_cast<int*>(t.b_tile + kSlices * kSmallBTile);
-  t.eb = t.ea + 32;
+  t.eb = t.ea + 64;
   t.bar = reinterpret_cast<uint64_t*>(t.eb + 32);
   t.abort = abort_flag;
   t.uses[0] = t.uses[1] = 0;
@@ -113,34 +113,30 @@ __device__ __forceinline__ void small_wait(SmallTC& t, int b) {
   if (!ok) *t.abort = 1;
 }
 
-// out(i, c, part, value): epilogue per real component of C = op(A) op(B).
-// Returns false (results not written) when a wait gave up; every thread of
-// the CTA calls it.
+// Two products with a shared right operand in one M = 128 tile:
+//   C0 = op(A0) op(B) (rows 0..2m-1 of the tile), C1 = op(A1) op(B) (rows
+//   64..64+2m-1).  out(k, i, c, part, value) receives every real component
+// of Ck.  Returns false (results not written) when a wait gave up; every
+// thread of the CTA calls it (256 threads: the eight warps drain TMEM).
 template <class Out>
-__device__ bool small_zgemm(SmallTC& t, int m, Op<double> A, Op<double> B, const Out& out) {
+__device__ bool small_zgemm2(SmallTC& t, int m, Op<double> A0, Op<double> A1, Op<double> B, const Out& out) {
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
-  // exponents: rows of op(A) (threads 0..m-1), columns of op(B) (threads 32..32+m-1)
-  if (tid < m) {
+  // exponents: rows of op(A0) (threads 0..m-1), op(A1) (32..), columns of op(B) (64..)
+  if (tid < 96 && (tid & 31) < m) {
+    const int k = tid >> 5, r = tid & 31;
     unsigned long long mx = 0;
     for (int j = 0; j < m; ++j) {
-      const cx<double> a = A.at(tid, j);
+      const cx<double> a = k == 0 ? A0.at(r, j) : (k == 1 ? A1.at(r, j) : B.at(j, r));
       const unsigned long long x = mag_bits(a.x), y = mag_bits(a.y);
       mx = x > mx ? x : mx;
       mx = y > mx ? y : mx;
     }
-    t.ea[tid] = exp_of_maxbits(mx);
-  } else if (tid >= 32 && tid < 32 + m) {
-    const int c = tid - 32;
-    unsigned long long mx = 0;
-    for (int j = 0; j < m; ++j) {
-      const cx<double> b = B.at(j, c);
-      const unsigned long long x = mag_bits(b.x), y = mag_bits(b.y);
-      mx = x > mx ? x : mx;
-      mx = y > mx ? y : mx;
-    }
-    t.eb[c] = exp_of_maxbits(mx);
+    if (k < 2)
+      t.ea[k * 32 + r] = exp_of_maxbits(mx);
+    else
+      t.eb[r] = exp_of_maxbits(mx);
   }
-  // the previous product's MMAs may still read the B tiles: wait for both buffers
+  // the previous product's MMAs may still read the tiles: wait for both buffers
   small_wait(t, 0);
   small_wait(t, 1);
   __syncthreads();
@@ -170,16 +166,19 @@ __device__ bool small_zgemm(SmallTC& t, int m, Op<double> A, Op<double> B, const
     if (s >= 2) small_wait(t, buf);
     __syncthreads();
     unsigned char* at = t.a_tile + buf * kSmallATile;
-    for (int idx = tid; idx < m * m; idx += nt) {
-      const int i = idx % m, j = idx / m;
-      const cx<double> a = A.at(i, j);
+    for (int idx = tid; idx < 2 * m * m; idx += nt) {
+      const int k = idx / (m * m), e = idx % (m * m);
+      const int i = e % m, j = e / m;
+      const cx<double> a = k == 0 ? A0.at(i, j) : A1.at(i, j);
+      const int ev = t.ea[k * 32 + i];
       bool nre, nim;
-      const unsigned long long Fr = fixed56(a.x, t.ea[i], nre);
-      const unsigned long long Fi = fixed56(a.y, t.ea[i], nim);
+      const unsigned long long Fr = fixed56(a.x, ev, nre);
+      const unsigned long long Fi = fixed56(a.y, ev, nim);
       const uint16_t re = slice_bf16(Fr, s + 1, nre), im = slice_bf16(Fi, s + 1, nim);
       const uint16_t mim = im ? (uint16_t)(im ^ 0x8000u) : (uint16_t)0;
-      *reinterpret_cast<uint32_t*>(at + sw_off(2 * i, 4 * j)) = (uint32_t)re | ((uint32_t)mim << 16);
-      *reinterpret_cast<uint32_t*>(at + sw_off(2 * i + 1, 4 * j)) = (uint32_t)im | ((uint32_t)re << 16);
+      const int row = k * 64 + 2 * i;
+      *reinterpret_cast<uint32_t*>(at + sw_off(row, 4 * j)) = (uint32_t)re | ((uint32_t)mim << 16);
+      *reinterpret_cast<uint32_t*>(at + sw_off(row + 1, 4 * j)) = (uint32_t)im | ((uint32_t)re << 16);
     }
     // make the generic-proxy writes visible to the tensor cores
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -206,13 +205,12 @@ __device__ bool small_zgemm(SmallTC& t, int m, Op<double> A, Op<double> B, const
   small_wait(t, 1);
   __syncthreads();
   const bool ok = *t.abort == 0;
-  if (ok) {
+  if (ok && nt >= 256) {
     tc_fence_after();
-    // lanes 0..63 hold the rows of Cbig: warps with (warp & 3) < 2, the
-    // upper warps of the pair taking columns 16..31
-    const int sub = warp & 3;
-    if (sub < 2 && nt >= 256) {
-      const int half = warp >> 2;
+    // warp w reads TMEM lanes 32 (w & 3) .. +31 (rows of the tile) and the
+    // column half w >> 2
+    const int sub = warp & 3, half = warp >> 2;
+    if (half < 2) {
       const int R = sub * 32 + lane;
       const uint32_t base = t.tmem + ((uint32_t)(sub * 32) << 16) + (uint32_t)(half * 16);
       long long F[16];
@@ -233,9 +231,10 @@ __device__ bool small_zgemm(SmallTC& t, int m, Op<double> A, Op<double> B, const
       }
       uint32_t r[16];
       tmem_ld16(base + (uint32_t)(kSmallLow * kSmallN), r);
-      const int i = R >> 1, part = R & 1;
-      if (R < 2 * m) {
-        const int ea = t.ea[i];
+      const int k = R >> 6, Rk = R & 63;
+      const int i = Rk >> 1, part = Rk & 1;
+      if (Rk < 2 * m) {
+        const int ea = t.ea[k * 32 + i];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int c = half * 16 + j;
@@ -246,7 +245,7 @@ __device__ bool small_zgemm(SmallTC& t, int m, Op<double> A, Op<double> B, const
             v = __longlong_as_double(0x7FF8000000000000ll);
           else
             v = scalbn((double)F[j] * 0x1p-42 + (double)__uint_as_float(r[j]), ea + eb);
-          out(i, c, part, v);
+          out(k, i, c, part, v);
         }
       }
     }
@@ -256,30 +255,22 @@ __device__ bool small_zgemm(SmallTC& t, int m, Op<double> A, Op<double> B, const
   return ok;
 }
 
-// Epilogues of the decimation step (component-wise: part 0 real, 1 imaginary)
-struct OutStore {
-  cx<double>* c;
+// Epilogues of the decimation step (component-wise: part 0 real, 1
+// imaginary; k selects the stacked product)
+enum { OUT_STORE = 0, OUT_ACC = 1, OUT_ACC2 = 2 };
+struct OutPair {
+  int mode[2];
+  cx<double>* c[2];
+  cx<double>* c2[2];  // second target of OUT_ACC2
   int ld;
-  __device__ __forceinline__ void operator()(int i, int j, int part, double v) const {
-    double* p = reinterpret_cast<double*>(c + i + j * ld);
-    p[part] = v;
-  }
-};
-struct OutAcc {
-  cx<double>* c;
-  int ld;
-  __device__ __forceinline__ void operator()(int i, int j, int part, double v) const {
-    double* p = reinterpret_cast<double*>(c + i + j * ld);
-    p[part] += v;
-  }
-};
-struct OutAcc2 {
-  cx<double>* c1;
-  cx<double>* c2;
-  int ld;
-  __device__ __forceinline__ void operator()(int i, int j, int part, double v) const {
-    reinterpret_cast<double*>(c1 + i + j * ld)[part] += v;
-    reinterpret_cast<double*>(c2 + i + j * ld)[part] += v;
+  __device__ __forceinline__ void operator()(int k, int i, int j, int part, double v) const {
+    double* p = reinterpret_cast<double*>(c[k] + i + j * ld) + part;
+    if (mode[k] == OUT_STORE) {
+      *p = v;
+    } else {
+      *p += v;
+      if (mode[k] == OUT_ACC2) reinterpret_cast<double*>(c2[k] + i + j * ld)[part] += v;
+    }
   }
 };
 
