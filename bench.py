@@ -213,13 +213,13 @@ def time_steps(torch, fn, steps, flush, stream):
     return times
 
 
-def large_block_sample(torch, sizes=((2, 8, 32), (3, 4, 8), (4, 2, 4))):
+def large_block_sample(torch, sizes=((2, 8, 32), (3, 8, 20), (4, 2, 4))):
     """Large-block engine on diamond-slab stacks (first + second neighbour
     springs, 28 / 72.6 mass blocks of 10 layers, L = 60): the plain FP64
     path (SIMT FP64 block products), the tensor-core path (the same FP64
     algorithm with every block product on tcgen05 as exact BF16 slice
     products) and the double-float engine, on n = 96 (8 transverse k x 32
-    omega), n = 216 (4 x 8) and n = 384 (2 x 4)."""
+    omega), n = 216 (8 x 20) and n = 384 (2 x 4)."""
     from phinfortran_gb300 import systems as S, transport_tdb
     out = []
     for nc, nk, ne in sizes:
@@ -317,6 +317,7 @@ def main():
                     help="skip the FP64 comparison path (accuracy and speed-up fields)")
     ap.add_argument("--no-grad", action="store_true", help="skip the gradient / forward cost ratio")
     ap.add_argument("--no-large", action="store_true", help="skip the large-block (diamond slab) sample")
+    ap.add_argument("--no-graph", action="store_true", help="time direct launches instead of a CUDA-graph replay")
     ap.add_argument("--energies", type=int, default=0,
                     help="use only N energies of the workload (profiling runs)")
     args = ap.parse_args()
@@ -360,14 +361,32 @@ def main():
     status = main_dt.status[:npts].cpu().numpy()
     T_main = main_dt.transl[:npts].cpu().numpy().copy()
 
+    # the step is captured once into a CUDA graph and replayed (no host work
+    # inside the timed region); the direct launch sequence is timed beside it
+    graph = None
+    if not args.no_graph:
+        try:
+            graph = main_dt.capture(Ed)
+            graph.replay()
+            torch.cuda.synchronize()
+            if not np.array_equal(main_dt.transl[:npts].cpu().numpy(), T_main):
+                graph = None
+        except RuntimeError:
+            graph = None
+    step_fn = (lambda: graph.replay()) if graph is not None else (lambda: main_dt.run(Ed, stream=stream))
+
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
-    times = time_steps(torch, lambda: main_dt.run(Ed, stream=stream), args.steps, flush, stream)
+    times = time_steps(torch, step_fn, args.steps, flush, stream)
     barrier()
     clk = clocks.stop()
     t_step = max_over_ranks(sum(times) / len(times))
     value = ws * npts / t_step
+    t_direct = None
+    if graph is not None:
+        td = time_steps(torch, lambda: main_dt.run(Ed, stream=stream), max(1, min(args.steps, 3)), flush, stream)
+        t_direct = sum(td) / len(td)
 
     # ---- FP64 comparison path: speed-up and accuracy of the headline path ----
     compare = None
@@ -399,6 +418,25 @@ def main():
                           max_where_fp64_reproducible=float(rel[good].max()) if good.any() else None,
                           note="points are 'fp64 reproducible' when a 1e-15 relative perturbation of the inputs "
                                "moves the FP64 result by <= 1e-10 relative"))
+        # the faster lead arithmetics of the mixed path, for the record
+        if args.path == "mixed":
+            variants = {}
+            for lead in ("split", "df64"):
+                dv = DeviceTransport(b, npts, want_transr=False, precision="mixed", refine_iters=args.refine,
+                                     lead_arith=lead, **p)
+                dv.run(Ed, stream=stream)
+                torch.cuda.synchronize()
+                tv = time_steps(torch, lambda: dv.run(Ed, stream=stream), max(1, min(args.steps, 3)), flush, stream)
+                rv = np.abs(dv.transl[:npts].cpu().numpy() - T64) / np.maximum(np.abs(T64), 1e-3)
+                variants[lead] = dict(ms_per_step=1e3 * sum(tv) / len(tv), solves_per_s=npts / (sum(tv) / len(tv)),
+                                      frac_le_1e_8=float((rv <= 1e-8).mean()),
+                                      frac_le_1e_8_where_fp64_reproducible=float((rv[good] <= 1e-8).mean()),
+                                      max_where_fp64_reproducible=float(rv[good].max()))
+                del dv
+            compare["lead_arith_variants"] = variants
+            compare["lead_arith_note"] = ("headline: FP64-grade lead decimations (block products on tcgen05 as "
+                                          "exact BF16 slice products, FP64 inverse); split = first 8 decimation "
+                                          "steps in FP64 then double-float; df64 = double-float decimations")
 
     # ---- gradient cost vs forward cost on the differentiable-conductance workload ----
     grad = None
@@ -457,9 +495,10 @@ def main():
         pipe_src = ("cuBLAS CGEMM 4096^3 (FP32 SIMT, TF32 off) measured live on this GPU: the 32-wide mixed "
                     "pipeline runs its matrix work on the FP32 pipe (FP32 and double-float arithmetic); the tensor "
                     "cores carry the large-block path (large_blocks)")
-        kernel = ("mixed pipeline per step: leads_kernel (double-float decimation, CTA per point) + layer_kernel "
-                  "(warp per point: FP32 LU, back substitution, refinement corrections, Caroli; the adaptive second "
-                  "sweep with a CTA per listed point) + residual_kernel; achieved = F per step / step time")
+        kernel = ("mixed pipeline per step (one CUDA-graph replay): leads_tc_kernel (FP64-grade decimation, "
+                  "its block products on tcgen05, one CTA per SM) + layer_kernel (warp per point: FP32 LU, back "
+                  "substitution, refinement corrections, Caroli; the adaptive second sweep with a CTA per listed "
+                  "point) + residual_kernel; achieved = F per step / step time")
     roof = dict(bound="tensor", achieved=achieved, peak=bf16_peak, unit="TFLOP/s", frac=achieved / bf16_peak,
                 traffic=None, peak_source=f"dense bf16 burst {peak_label} (MEASURED_PEAKS.json bf16_tflops)",
                 pipe=pipe, pipe_peak=pipe_peak, pipe_frac=achieved / pipe_peak, pipe_peak_source=pipe_src,
@@ -488,11 +527,15 @@ def main():
         launches_per_step = 8 + 7 + 1 + 1 + 1 + sweeps + 1
     line = dict(metric=METRIC, value=value, unit="solves/s", n_gpus=ws, steps=args.steps, warmup=args.warmup,
                 ms_per_step=t_step * 1e3, higher_is_better=True, scaling="weak", vs_baseline=None,
-                dtype="complex128 (fp64)" if args.path == "fp64" else "complex: fp32 + double-float (no fp64 ops)",
+                dtype="complex128 (fp64)" if args.path == "fp64" else
+                ("complex: FP64-grade leads (tcgen05 bf16 slice products, fp64 inverse) + fp32 factorisation "
+                 "+ double-float refinement"),
                 data="synthetic (seeded PCG64)",
                 config=dict(workload=WORKLOAD["workload"], n=n, L=L, energies=npts, eta=1e-6, path=args.path,
                             refine_iters=args.refine if args.path == "mixed" else None,
-                            l2="flushed (256 MB write) before every timed step", parallelism=f"replicas x{ws}"),
+                            l2="flushed (256 MB write) before every timed step", parallelism=f"replicas x{ws}",
+                            timed="one CUDA-graph replay per step" if graph is not None else "direct launches"),
+                direct_launch_ms_per_step=None if t_direct is None else t_direct * 1e3,
                 e2e=dict(value=e2e_value, unit="solves/s", h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
                          entry="pf_transport_tdb_mixed" if args.path == "mixed" else "pf_transport_tdb"),
                 roofline=roof, cpu_baseline=cpu, compare=compare, gradient=grad, large_blocks=large,
