@@ -433,6 +433,42 @@ int pf_transport_tdb_modes_ex_dev(int n, int nl, int nr, int L, int nq,
                                   void* work, size_t work_bytes,
                                   void* stream);
 
+/*
+ * The FP64 transport of one batch (T_L, T_R, status) plus the Green's
+ * functions that the reference's vel_mat_tdb receives from
+ * surface_green_tdb_mpi (negf/surface.f90:344-383: the four decimations)
+ * and get_G_full_tdb_mpi (negf/lesser.f90:100-157), for drivers that keep
+ * their own mode analysis.  Per point, column-major complex(kind=8), each
+ * output optional (null: not written):
+ *   gl_adv, gl_plus    [npts][nl][nl]  left surface functions (advanced,
+ *                                      and the "plus" problem of :510-532)
+ *   gr_ret, gr_minus   [npts][nr][nr]  right (retarded, "minus" :571-593)
+ *   gml_adv [npts][nl][nl], gmr_ret [npts][nr][nr]   broadenings
+ *                                      i (Sigma - Sigma^H)
+ *   G_D_LR  [npts][nl][nr]  G_{0,N+1}     G_R [npts][nr][nr]  G_{N+1,N+1}
+ *   G_D_RL  [npts][nr][nl]  G_{N+1,0}     G_L [npts][nl][nl]  G_{0,0}
+ * The workspace is that of the mode-resolved entry
+ * (pf_transport_tdb_blocks_workspace_size); errors are reported through
+ * pf_modes_last_error.
+ */
+size_t pf_transport_tdb_blocks_workspace_size(int n, int nl, int nr, int nq, int npts);
+
+int pf_transport_tdb_blocks_dev(int n, int nl, int nr, int L, int nq,
+                                const double* HL, const double* HLv,
+                                const double* HR, const double* HRv,
+                                const double* Hd, const double* Hdv,
+                                const double* Hld, const double* Hrd,
+                                int npts, const double* E, const int* qidx,
+                                const int* zero_flag, double eta, double eta0,
+                                double dev_factor, double convergence,
+                                int max_iter, double* transl, double* transr,
+                                int* status, double* gl_adv, double* gl_plus,
+                                double* gr_ret, double* gr_minus,
+                                double* gml_adv, double* gmr_ret,
+                                double* G_D_LR, double* G_R, double* G_D_RL,
+                                double* G_L, void* work, size_t work_bytes,
+                                void* stream);
+
 /* Message for the last error of the mode-resolved entry points. */
 const char* pf_modes_last_error(void);
 
@@ -481,11 +517,12 @@ const char* pf_tiled_last_error(void);
  *     C_b = alpha op(A_b) op(B_b) + beta C_b,   b = 0 .. batch-1,
  * op = 'N' or 'C' (conjugate transpose), complex(kind=8) column-major
  * device arrays, real alpha and beta, batch strides in complex elements
- * (0 shares an operand).  Every row of op(A) and column of op(B) is scaled
- * by a power of two and split into eight 7-bit BF16 slices; the slice
- * products that matter are summed exactly on the tensor cores (FP32
- * accumulation of integers below 2^22) and assembled in FP64, so the
- * result has the accuracy of an FP64 GEMM (error O(k 2^-55) |A| |B|).
+ * (0 shares an operand), 1 <= k <= 2048 (PF_ERR_SIZE above).  Every row
+ * of op(A) and column of op(B) is scaled by a power of two and split into
+ * nine 7-bit BF16 slices (63 bits); the slice products that matter are
+ * summed exactly on the tensor cores (FP32 accumulation of integers below
+ * 2^22) and assembled in FP64, so the result has the accuracy of an FP64
+ * GEMM (error O(k 2^-55) |A| |B|).
  * work: pf_tc_zgemm_workspace_size bytes of device memory (a_shared /
  * b_shared: strideA / strideB == 0).  Synchronous on `stream`.
  */

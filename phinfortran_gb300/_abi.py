@@ -77,6 +77,14 @@ SIGNATURES = {
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_size_t, C.c_void_p]),
     "pf_modes_last_error": (C.c_char_p, []),
+    "pf_transport_tdb_blocks_workspace_size": (C.c_size_t, [C.c_int] * 5),
+    "pf_transport_tdb_blocks_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                              C.c_void_p, C.c_void_p, C.c_void_p]
+                                    + [C.c_void_p] * 10 + [C.c_void_p, C.c_size_t, C.c_void_p]),
     "pf_transport_tdb_modes_workspace_size": (C.c_size_t, [C.c_int] * 5),
     "pf_transport_tdb_modes_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -193,6 +193,138 @@ __device__ void copy_cvt(cx<A>* dst, int ldd, bool conj_t, const cx<B>* src, int
 // products per step on the tensor cores (FP64-grade slice products, see
 // tc_small.cuh) and the inverse in FP64 on the CTA.  On return SM2 holds
 // g = inv(z - es) and G_ES holds es (FP64), as after decimate<double>.
+// FP64 Gauss-Jordan inverse of an n x n block (n <= 32) for the
+// tensor-core decimation, by a CTA of 256 threads, with look-ahead.  The
+// matrix alternates between M and T (step k reads one and writes the other,
+// so nothing is read after it is overwritten) and a step needs one barrier:
+// warp 0 writes column k+1 of step k's result, picks the pivot of step k+1
+// (first maximum of |re| + |im| among the unused rows, as inverse()) and
+// forms its reciprocal and the multipliers f(r) = a(r, k+1) / pivot, while
+// warps 1-7 write the other columns.  Elimination in multiplier form:
+// a'(r, c) = a(r, c) - f(r) a(p, c), a'(p, c) = a(p, c) / pivot,
+// a'(r, k) = -f(r), a'(p, k) = 1 / pivot.  The row and column order is
+// restored by one gather, inv(k, P(j)) = A(P(k), j).  fbuf holds two
+// buffers of m multipliers (the pivot row's entry carries 1 / pivot); the
+// status bits (PF_SINGULAR, PF_NAN) are those of inverse().
+struct LaWork {
+  cx<double>* f;  // [2 m]
+  int* perm;      // [n]
+  int* flag;      // [1]
+  int m;
+};
+
+__device__ __forceinline__ cx<double> la_recip(cx<double> a) {
+  // 1 / a = conj(a) / |a|^2 with a scaled by s = 2^-e, 2^e <= max(|re|, |im|)
+  // < 2^(e+1), so that |a s|^2 neither overflows nor underflows
+  const double mx = fmax(fabs(a.x), fabs(a.y));
+  if (!(mx > 0.0) || !(mx <= 1.7976931348623157e308)) {
+    const double nan = __longlong_as_double(0x7FF8000000000000ll);
+    return mk<double>(nan, nan);
+  }
+  const int e = ilogb(mx);
+  if (e < -1020 || e > 1020) return crecip(a);  // scale factor out of range: Smith's form
+  const double sc = scalbn(1.0, -e);
+  const double sx = a.x * sc, sy = a.y * sc;
+  const double r = 1.0 / fma(sx, sx, sy * sy);
+  return mk<double>(sx * r * sc, -sy * r * sc);
+}
+
+// Warp 0: pivot of the column v (lane r holds row r) among the unused rows;
+// writes the multipliers, 1 / pivot at the pivot's slot and perm[k].
+__device__ __forceinline__ int la_pivot(cx<double> v, int lane, int n, bool used, cx<double>* f, int* perm_k) {
+  const double a = cabs1(v);
+  double best = (lane < n && !used) ? ((a != a) ? 3.0e300 : a) : -1.0;
+  int bi = (lane < n && !used) ? lane : 64;
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (ob > best || (ob == best && oi < bi)) {
+      best = ob;
+      bi = oi;
+    }
+  }
+  const int p = bi < n ? bi : 0;
+  const cx<double> piv = mk<double>(__shfl_sync(0xffffffffu, v.x, p), __shfl_sync(0xffffffffu, v.y, p));
+  int st = PF_OK;
+  if (piv.x == 0.0 && piv.y == 0.0) st |= PF_SINGULAR;
+  if (!(isfinite(piv.x) && isfinite(piv.y))) st |= PF_NAN;
+  const cx<double> ip = la_recip(piv);
+  if (lane < n) f[lane] = lane == p ? ip : cmul(v, ip);
+  if (lane == 0) *perm_k = p;
+  return st;
+}
+
+__device__ int inverse_la(cx<double>* M, cx<double>* T, int ld, int n, LaWork w) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  int st = PF_OK;
+  bool used = false;  // warp 0, lane r: row r has been a pivot
+  if (warp == 0) st |= la_pivot(lane < n ? M[lane] : mk<double>(0.0, 0.0), lane, n, false, w.f, w.perm);
+  __syncthreads();
+  cx<double>* src = M;
+  cx<double>* dst = T;
+  for (int k = 0; k < n; ++k) {
+    const cx<double>* f = w.f + (k & 1) * w.m;
+    const int p = w.perm[k];
+    const cx<double> ip = f[p];
+    if (warp == 0) {
+      if (k + 1 < n) {
+        cx<double> v = mk<double>(0.0, 0.0);
+        if (lane < n) {
+          const cx<double> ap = src[p + (k + 1) * ld];
+          if (lane == p) {
+            v = cmul(ap, ip);
+          } else {
+            const cx<double> fr = f[lane];
+            v = src[lane + (k + 1) * ld];
+            v.x = fma(-fr.x, ap.x, fma(fr.y, ap.y, v.x));
+            v.y = fma(-fr.x, ap.y, fma(-fr.y, ap.x, v.y));
+          }
+          dst[lane + (k + 1) * ld] = v;
+        }
+        if (lane == p) used = true;
+        st |= la_pivot(v, lane, n, used, w.f + ((k + 1) & 1) * w.m, w.perm + k + 1);
+      }
+    } else {
+      for (int i = tid - 32; i < n * n; i += nt - 32) {
+        const int r = i % n, c = i / n;
+        if (c == k + 1) continue;
+        cx<double> o;
+        if (c == k) {
+          o = r == p ? ip : mk<double>(-f[r].x, -f[r].y);
+        } else if (r == p) {
+          o = cmul(src[p + c * ld], ip);
+        } else {
+          const cx<double> fr = f[r], a = src[p + c * ld];
+          o = src[r + c * ld];
+          o.x = fma(-fr.x, a.x, fma(fr.y, a.y, o.x));
+          o.y = fma(-fr.x, a.y, fma(-fr.y, a.x, o.y));
+        }
+        dst[r + c * ld] = o;
+      }
+    }
+    __syncthreads();
+    cx<double>* t = src;
+    src = dst;
+    dst = t;
+  }
+  // src holds the permuted inverse
+  for (int i = tid; i < n * n; i += nt) {
+    const int r = i % n, c = i / n;
+    dst[r + w.perm[c] * ld] = src[w.perm[r] + c * ld];
+  }
+  if (tid == 0) *w.flag = st;
+  __syncthreads();
+  if (dst != M) {
+    for (int i = tid; i < n * n; i += nt) {
+      const int r = i % n, c = i / n;
+      M[r + c * ld] = dst[r + c * ld];
+    }
+  }
+  st = *w.flag;
+  __syncthreads();
+  return st;
+}
+
 template <int S>
 __device__ int decimate_tc(const Ctx<double>& c, tc::SmallTC& t, int m, cx<double> z, Op<double> h00,
                            Op<double> a0, Op<double> b0, double conv, int max_iter, int* iters_out) {
@@ -205,6 +337,9 @@ __device__ int decimate_tc(const Ctx<double>& c, tc::SmallTC& t, int m, cx<doubl
   cx<double>* W2 = c.gs[G_W2];
   cx<double>* W3 = c.gs[G_W3];
   int st = PF_OK;
+  // look-ahead inverse: the multipliers in the inverse workspace (rowk and
+  // colk are contiguous, 2 m entries), the second matrix buffer in SM3
+  const LaWork la{c.iw.rowk, c.iw.perm, c.iw.flag, m};
   copy_in(e1, ld, h00, m, m);
   copy_in(es, ld, h00, m, m);
   copy_in(al, ld, a0, m, m);
@@ -217,27 +352,44 @@ __device__ int decimate_tc(const Ctx<double>& c, tc::SmallTC& t, int m, cx<doubl
       break;
     }
     shift_neg(W1, ld, z, e1, ld, m);                                                 // z - e1
-    st |= inverse(W1, ld, m, c.iw);                                                  // ive
-    // the six products of a step as three stacked pairs sharing the right operand:
-    //   [A; B] = [alpha; beta] ive,  e1, es += A beta with beta' = B beta,
-    //   alpha' = A alpha with e1 += B alpha
-    using tc::OutPair;
-    bool ok = tc::small_zgemm2(t, m, opN<double>(al, ld), opN<double>(be, ld), opN<double>(W1, ld),
-                               OutPair{{tc::OUT_STORE, tc::OUT_STORE}, {W2, W3}, {nullptr, nullptr}, ld});
-    ok = ok && tc::small_zgemm2(t, m, opN<double>(W2, ld), opN<double>(W3, ld), opN<double>(be, ld),
-                                OutPair{{tc::OUT_ACC2, tc::OUT_STORE}, {e1, be}, {es, nullptr}, ld});
-    ok = ok && tc::small_zgemm2(t, m, opN<double>(W2, ld), opN<double>(W3, ld), opN<double>(al, ld),
-                                OutPair{{tc::OUT_STORE, tc::OUT_ACC}, {al, e1}, {nullptr, nullptr}, ld});
+    st |= inverse_la(W1, c.sm[3], ld, m, la);                                        // ive
+    // the six products of a step as two tensor-core calls:
+    //   [W2; W3] = [alpha; beta] ive, then
+    //   [W2; W3] [beta alpha] = [W2 beta, W2 alpha; W3 beta, W3 alpha]:
+    //   e1, es += W2 beta; alpha' = W2 alpha; beta' = W3 beta; e1 += W3 alpha
+    // (the last through W3, whose values are in registers by then, so that
+    // e1 receives its two sums in the order of the FP64 step)
+    using tc::OutQuad;
+    const Op<double> b1[1] = {opN<double>(W1, ld)};
+    bool ok = tc::small_zgemm<1>(t, m, opN<double>(al, ld), opN<double>(be, ld), b1,
+                                 OutQuad{{{tc::OUT_STORE, 0}, {tc::OUT_STORE, 0}},
+                                         {{W2, nullptr}, {W3, nullptr}},
+                                         {{nullptr, nullptr}, {nullptr, nullptr}},
+                                         ld});
+    const Op<double> b2[2] = {opN<double>(be, ld), opN<double>(al, ld)};
+    ok = ok && tc::small_zgemm<2>(t, m, opN<double>(W2, ld), opN<double>(W3, ld), b2,
+                                  OutQuad{{{tc::OUT_ACC2, tc::OUT_STORE}, {tc::OUT_STORE, tc::OUT_STORE}},
+                                          {{e1, al}, {be, W3}},
+                                          {{es, nullptr}, {nullptr, nullptr}},
+                                          ld});
     if (!ok) {
       st |= PF_TC_TIMEOUT;
       break;
     }
+    for (int i = threadIdx.x; i < m * m; i += blockDim.x) {
+      const int r = i % m, cc = i / m;
+      const cx<double> w = W3[r + cc * ld];
+      cx<double>& e = e1[r + cc * ld];
+      e.x += w.x;
+      e.y += w.y;
+    }
+    __syncthreads();
     maxdiff = max_abs(al, ld, m, m, c.red);
     ++it;
   }
   if (maxdiff != maxdiff) st |= PF_NAN;
   shift_neg(W1, ld, z, es, ld, m);
-  st |= inverse(W1, ld, m, c.iw);
+  st |= inverse_la(W1, c.sm[3], ld, m, la);
   if (iters_out) *iters_out = it;
   return st;
 }

@@ -579,6 +579,23 @@ int prep_grid(const MLayout& lay, int npts, int S) {
   return g < npts ? g : npts;
 }
 
+// Packed per-point outputs of pf_transport_tdb_blocks_dev: record k of a
+// chunk (leading dimension ld) -> dst[k] + p * rows[k] * cols[k]
+// (column-major), for the records whose dst is set.
+struct BlockOut {
+  double* dst[NREC];
+  int rows[NREC], cols[NREC];
+};
+
+__global__ void blocks_out_kernel(Chunk ch, int p0, int cnt, int ld, BlockOut bo) {
+  const int lp = blockIdx.x, k = blockIdx.y;
+  if (lp >= cnt || bo.dst[k] == nullptr) return;
+  const int rows = bo.rows[k], cols = bo.cols[k];
+  const C* src = ch.rec(lp, k);
+  C* d = reinterpret_cast<C*>(bo.dst[k]) + (size_t)(p0 + lp) * rows * cols;
+  for (int i = threadIdx.x; i < rows * cols; i += blockDim.x) d[i] = src[i % rows + (i / rows) * ld];
+}
+
 size_t modes_bytes(const MLayout& lay, int nq, int chunk, int grid) {
   const size_t mir = ((size_t)nq * 4 + 255) & ~(size_t)255;
   return 256 + mir + (size_t)grid * lay.per_cta + (size_t)chunk * lay.per_point;
@@ -693,6 +710,92 @@ int pf_transport_tdb_modes_ex_dev(int n, int nl, int nr, int L, int nq, const do
     MD_CUDA(cudaGetLastError());
     tr_kernel<<<cnt, kTaskThreads, lay.task_smem, st>>>(sys, pts, p0, cnt, lay, ch, geo, eta, eta0, out);
     MD_CUDA(cudaGetLastError());
+  }
+  return PF_SUCCESS;
+}
+
+size_t pf_transport_tdb_blocks_workspace_size(int n, int nl, int nr, int nq, int npts) {
+  return pf_transport_tdb_modes_workspace_size(n, nl, nr, nq, npts);
+}
+
+int pf_transport_tdb_blocks_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
+                                const double* HR, const double* HRv, const double* Hd, const double* Hdv,
+                                const double* Hld, const double* Hrd, int npts, const double* E, const int* qidx,
+                                const int* zero_flag, double eta, double eta0, double dev_factor,
+                                double convergence, int max_iter, double* transl, double* transr, int* status,
+                                double* gl_adv, double* gl_plus, double* gr_ret, double* gr_minus, double* gml_adv,
+                                double* gmr_ret, double* G_D_LR, double* G_R, double* G_D_RL, double* G_L,
+                                void* work, size_t work_bytes, void* stream) {
+  if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0)
+    return set_err(PF_ERR_ARG, "pf_blocks: dimensions must be positive");
+  if (n > PF_NMAX_RESIDENT || nl > PF_NMAX_RESIDENT || nr > PF_NMAX_RESIDENT)
+    return set_err(PF_ERR_SIZE, "pf_blocks: block size exceeds the resident kernel limit");
+  if (!HL || !HLv || !HR || !HRv || !Hd || !Hld || !Hrd || (L > 1 && !Hdv))
+    return set_err(PF_ERR_ARG, "pf_blocks: null block pointer");
+  if (!E || !transl || !status) return set_err(PF_ERR_ARG, "pf_blocks: null pointer");
+  if (max_iter <= 0) return set_err(PF_ERR_ARG, "pf_blocks: bad max_iter");
+  if (npts == 0) return PF_SUCCESS;
+  const MLayout lay = mlayout(n, nl, nr);
+  const int S = (lay.m + 31) / 32;
+  const int chunk = npts < kChunk ? npts : kChunk;
+  const int grid = prep_grid(lay, chunk, S);
+  if (grid <= 0) return set_err(PF_ERR_SIZE, "pf_blocks: kernel does not fit on the device");
+  if (!work || work_bytes < modes_bytes(lay, nq, chunk, grid))
+    return set_err(PF_ERR_ARG, "pf_blocks: workspace too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  int* queue = reinterpret_cast<int*>(work);
+  const size_t mir = ((size_t)nq * 4 + 255) & ~(size_t)255;
+  int* mirror = reinterpret_cast<int*>(reinterpret_cast<char*>(work) + 256);
+  char* gscr = reinterpret_cast<char*>(work) + 256 + mir;
+  Chunk ch;
+  ch.base = gscr + (size_t)grid * lay.per_cta;
+  ch.per_point = lay.per_point;
+  ch.mat = lay.mat;
+  pf::System<double> sys;
+  sys.n = n;
+  sys.nl = nl;
+  sys.nr = nr;
+  sys.L = L;
+  sys.nq = nq;
+  sys.HL = reinterpret_cast<const cx<double>*>(HL);
+  sys.HLv = reinterpret_cast<const cx<double>*>(HLv);
+  sys.HR = reinterpret_cast<const cx<double>*>(HR);
+  sys.HRv = reinterpret_cast<const cx<double>*>(HRv);
+  sys.Hd = reinterpret_cast<const cx<double>*>(Hd);
+  sys.Hdv = reinterpret_cast<const cx<double>*>(Hdv);
+  sys.Hld = reinterpret_cast<const cx<double>*>(Hld);
+  sys.Hrd = reinterpret_cast<const cx<double>*>(Hrd);
+  pf::Points pts{npts, E, qidx, zero_flag};
+  pf::Params P{nullptr, eta, eta0, dev_factor, convergence, max_iter, 1};
+  if (nl == nr) {
+    mirror_kernel<<<nq, 256, 0, st>>>(HL, HLv, HR, HRv, 2 * nl * nl, nq, mirror);
+    P.lead_mirror = mirror;
+  }
+  ModeOut out{transl, transr, nullptr, status, nullptr, nullptr, nullptr, nullptr, nl > nr ? nl : nr};
+  BlockOut bo;
+  double* const dst[NREC] = {gl_adv, gl_plus, gr_ret, gr_minus, gml_adv, gmr_ret, G_D_LR, G_R, G_D_RL, G_L};
+  const int rows[NREC] = {nl, nl, nr, nr, nl, nr, nl, nr, nr, nl};
+  const int cols[NREC] = {nl, nl, nr, nr, nl, nr, nr, nr, nl, nl};
+  bool any = false;
+  for (int k = 0; k < NREC; ++k) {
+    bo.dst[k] = dst[k];
+    bo.rows[k] = rows[k];
+    bo.cols[k] = cols[k];
+    any = any || dst[k] != nullptr;
+  }
+  for (int p0 = 0; p0 < npts; p0 += chunk) {
+    const int cnt = (npts - p0) < chunk ? (npts - p0) : chunk;
+    MD_CUDA(cudaMemsetAsync(queue, 0, sizeof(int), st));
+    const int g = grid < cnt ? grid : cnt;
+    if (S == 1)
+      prep_kernel<1><<<g, kPrepThreads, lay.prep_smem, st>>>(sys, pts, p0, cnt, P, lay, ch, gscr, queue, out);
+    else
+      prep_kernel<2><<<g, kPrepThreads, lay.prep_smem, st>>>(sys, pts, p0, cnt, P, lay, ch, gscr, queue, out);
+    MD_CUDA(cudaGetLastError());
+    if (any) {
+      blocks_out_kernel<<<dim3(cnt, NREC), 256, 0, st>>>(ch, p0, cnt, lay.ld, bo);
+      MD_CUDA(cudaGetLastError());
+    }
   }
   return PF_SUCCESS;
 }

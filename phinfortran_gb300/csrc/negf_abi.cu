@@ -513,11 +513,17 @@ __global__ void __launch_bounds__(kThreads) leads_kernel(pf::MSys sys, pf::Point
 // Leads kernel of the FP64 lead arithmetic (blocks up to 32): the same work
 // as leads_kernel<1>, the decimations' block products on the tensor cores
 // (tc_small.cuh).  One CTA per SM: it holds all 512 TMEM columns (the
-// dynamic shared memory requested keeps a second CTA off the SM).
+// dynamic shared memory requested keeps a second CTA off the SM).  With
+// gs_smem the four working matrices of the decimation (e1, es and the two
+// products W2, W3) are in shared memory instead of the CTA's global
+// scratch: three after the tensor-core tiles, W3 in SM3 (the decimation's
+// inverse uses SM3 as its second buffer only while W3 is dead).
+constexpr int kLeadsTcShared = 3;  // M_E1, M_ES, M_W2 (M_W3 in SM3)
+static_assert(kThreads == pf::tc::kSmallThreads, "small_zgemm is written for the leads CTA size");
 __global__ void __launch_bounds__(kThreads, 1) leads_tc_kernel(pf::MSys sys, pf::Points pts, pf::Params P,
                                                          pf::Outputs out, MixedLayout lay, size_t per_cta,
                                                          char* scratch, pf::wp::LeadOut lo, int* lead_status,
-                                                         int* queue) {
+                                                         int* queue, int gs_smem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int S = 1;
   pf::MCtx c;
@@ -551,6 +557,12 @@ __global__ void __launch_bounds__(kThreads, 1) leads_tc_kernel(pf::MSys sys, pf:
   // tensor-core tiles after the decimation slots, 1024-aligned
   unsigned char* tiles = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + lay.smem_leads + 1023) & ~(uintptr_t)1023);
+  if (gs_smem) {
+    static_assert(pf::M_E1 == 0 && pf::M_ES == 1 && pf::M_W2 == 2 && pf::M_W3 == 3, "decimation slots first");
+    dcx* gsm = reinterpret_cast<dcx*>(tiles + pf::tc::kSmallSmem);
+    for (int i = 0; i < kLeadsTcShared; ++i) c.gs[i] = gsm + i * mat;
+    c.gs[pf::M_W3] = c.sm[3];
+  }
   pf::tc::SmallTC tcx;
   pf::tc::small_init(tcx, tiles, &s_tc_abort);
   for (;;) {
@@ -1501,11 +1513,15 @@ int mixed_launch(const MixedPlan& plan, int n, int nl, int nr, int L, int nq, co
     int* rcount = queue + 2;
     if (lead_mode == pf::PF_LEAD_FP64) {
       // tensor-core products in the FP64 decimations: one CTA per SM
-      const size_t smem_tc = lay.smem_leads + 1024 + (size_t)pf::tc::kSmallSmem;
+      const DevInfo di = device_info();
+      size_t smem_tc = lay.smem_leads + 1024 + (size_t)pf::tc::kSmallSmem;
+      const size_t gs_bytes = (size_t)kLeadsTcShared * lay.base.mat * sizeof(dcx);
+      const int gs_smem = smem_tc + gs_bytes <= di.smem_optin ? 1 : 0;
+      if (gs_smem) smem_tc += gs_bytes;
       PF_CUDA(cudaFuncSetAttribute(leads_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tc));
-      const int grid_tc = plan.grid_a < device_info().sms ? plan.grid_a : device_info().sms;
+      const int grid_tc = plan.grid_a < di.sms ? plan.grid_a : di.sms;
       leads_tc_kernel<<<grid_tc, kThreads, smem_tc, st>>>(sys, pts, P, out, lay, plan.per_cta_a, scratch, lo, lstat,
-                                                          queue);
+                                                          queue, gs_smem);
     } else {
       leads_kernel<1><<<plan.grid_a, kThreads, lay.smem_leads, st>>>(sys, pts, P, out, lay, plan.per_cta_a, scratch,
                                                                       lo, lstat, queue);

@@ -10,18 +10,24 @@
 //     so Cbig = Abig Bbig^T has Re c_ic in row 2i and Im c_ic in row 2i+1 --
 //     the interleaved (re, im) order of the complex(kind=8) output;
 //   * every row of op(A) (every column of op(B)) is scaled by a power of two
-//     2^-e (e: exponent of its largest entry), so |x| < 1, and x*2^56 is
-//     truncated to a 56-bit integer F (integer operations on the FP64 bits);
-//   * slice s = 1..8 holds q_s * 2^-7s with q_s the s-th 7-bit group of F
-//     (|q_s| <= 127: exact in BF16), so x = sum_s q_s 2^-7s + O(2^-56);
-//   * the product keeps the slice pairs with s + t <= 9.  For s + t <= 6 the
+//     2^-e (e: exponent of its largest entry), so |x| < 1, and x*2^63 is
+//     truncated to a 63-bit integer F (integer operations on the FP64 bits);
+//   * slice s = 1..9 holds q_s * 2^-7s with q_s the s-th 7-bit group of F
+//     (|q_s| <= 127: exact in BF16), so x = sum_s q_s 2^-7s + O(2^-63).
+//     An entry 2^-10 below the largest of its row still keeps all 53 bits;
+//     with eight slices (56 bits) the blocks of a wide multi-orbital ribbon,
+//     whose rows span several decades, gave T 2e-7 away from FP64;
+//   * the product keeps the slice pairs with s + t <= 10.  For s + t <= 7 the
 //     FP32 tensor-core sums over K chunks of 256 are integers below 2^22
 //     (127^2 * 256 < 2^22), hence exact; each chunk is drained from TMEM and
-//     added into a 64-bit fixed-point sum.  The pairs with s + t >= 7 weigh
-//     at most 2^-49 and share one FP32 accumulator over the whole K (the
-//     tensor cores' FP32 sums are not correctly rounded, so a heavier
-//     inexact chain would lose accuracy: with s + t >= 6 in it the products
-//     drifted by ~2^-42 relative).
+//     added into a 64-bit fixed-point sum (LSB 2^-49).  The pairs with
+//     s + t >= 8 weigh at most 2^-56 and share one FP32 accumulator over the
+//     whole K.  The tensor cores' FP32 sums are not correctly rounded: a long
+//     inexact chain drifts with a bias (about 2^-24 of the accumulator per
+//     MMA), so only light pairs may share it -- with the pairs of sum 7 in
+//     it the products were 7 (median) to 64 (maximum) units of 2^-53 |A| |B|
+//     away from the exact product on random inputs, against 0.2 to 0.6 for
+//     an FP64 GEMM, and a 768-wide ribbon's T moved by 2e-7.
 // The result is assembled in FP64 once per output element and scaled back
 // by 2^(e_row + e_col).  Relative to |A| |B| the error is O(K 2^-55), the
 // accuracy of an FP64 GEMM.
@@ -61,11 +67,21 @@ constexpr int kTmemCols = 2 * kBN;        // top slot [0, kBN), low slot [kBN, 2
 
 static_assert(kTmemCols >= 32 && (kTmemCols & (kTmemCols - 1)) == 0, "TMEM allocation must be a power of 2");
 static_assert(kChunk * 127 * 127 < (1 << 22), "exact chain bound");
-static_assert(kSlices * kBeta == 56, "56-bit fixed point");
-static_assert(kSlices + 1 > kTopD, "the low accumulator receives at least one pair per chunk");
-static_assert(kTopD * kBeta == 42, "fixed-point LSB used in the epilogue");
-// |F| <= chunks * (2^22 << 7 (kTopD - 2)) * pairs: with K <= 4096 (16 chunks) below 2^63
-static_assert(22 + kBeta * (kTopD - 2) + 4 + 4 < 63, "64-bit fixed-point range");
+static_assert(kSlicesL * kBeta == 63, "63-bit fixed point");
+constexpr int kTopDL = 7;  // largest exact pair sum (1-based) of the large products
+static_assert(kSlicesL + 1 > kTopDL, "the low accumulator receives at least one pair per chunk");
+static_assert(kTopDL * kBeta == 49, "fixed-point LSB used in the epilogue");
+// |F| <= chunks * sum_d (d - 1) (127^2 kChunk) 2^(7 (kTopDL - d)): about
+// 2^57 a chunk, so at most kMaxChunks chunks (K <= kMaxChunks kChunk real,
+// half of it complex) stay below 2^62
+constexpr int kMaxChunks = 16;
+constexpr double fixed_bound() {
+  double b = 0.0, w = 1.0;
+  for (int d = kTopDL; d >= 2; --d, w *= 128.0) b += (d - 1) * 127.0 * 127.0 * kChunk * w;
+  return b * kMaxChunks;
+}
+static_assert(fixed_bound() < 4.611686018427388e18, "64-bit fixed-point range (2^62)");
+static_assert(2 * kMaxK <= kMaxChunks * kChunk, "K limit of the public entry");
 
 // ---------------------------------------------------------------------------
 // TMA tile load (4-D map: K, rows, slice, batch)
@@ -155,13 +171,13 @@ __global__ void vec_slice(VecSet V, const int* active, const int* e, int kp, boo
     if (V.conj) a.y = -a.y;
   }
   bool nre, nim;
-  const unsigned long long Fr = fixed56(a.x, ev, nre);
-  const unsigned long long Fi = fixed56(a.y, ev, nim);
+  const unsigned long long Fr = fixed_pt<kSlicesL * kBeta>(a.x, ev, nre);
+  const unsigned long long Fi = fixed_pt<kSlicesL * kBeta>(a.y, ev, nim);
 #pragma unroll
-  for (int s = 1; s <= kSlices; ++s) {
-    const uint16_t re = slice_bf16(Fr, s, nre);
-    const uint16_t im = slice_bf16(Fi, s, nim);
-    const size_t plane = ((size_t)b * kSlices + (s - 1)) * rows;
+  for (int s = 1; s <= kSlicesL; ++s) {
+    const uint16_t re = slice_bf16_n<kSlicesL>(Fr, s, nre);
+    const uint16_t im = slice_bf16_n<kSlicesL>(Fi, s, nim);
+    const size_t plane = ((size_t)b * kSlicesL + (s - 1)) * rows;
     if (pair) {
       const uint16_t mim = im ? (uint16_t)(im ^ 0x8000u) : (uint16_t)0;
       uint32_t* r0 = reinterpret_cast<uint32_t*>(out + (plane + 2 * (size_t)v) * kp + 2 * j);
@@ -242,7 +258,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   for (int c = 0; c < nchunk && !abort; ++c) {
     const int k0 = c * kChunk;
     const int ks = min(kBoxes, (p.kp - k0) / kKStep);
-    for (int s = 0; s < kSlices && !abort; ++s) {
+    for (int s = 0; s < kSlicesL && !abort; ++s) {
       if (tid == 0) {
         mbar_expect_tx(bar_a, (uint32_t)(ks * kBoxA));
         for (int u = 0; u < ks; ++u) tma_load_4d(smem_u32(sA + u * kBoxA), &ta, k0 + u * kKStep, m0, s, ba, bar_a);
@@ -251,9 +267,9 @@ __global__ void __launch_bounds__(kThreads, 2)
       pend_bar = bar_a;
       pend_ph = ph_a;
       ph_a ^= 1;
-      for (int t = 0; s + t <= kSlices - 1 && !abort; ++t) {
+      for (int t = 0; s + t <= kSlicesL - 1 && !abort; ++t) {
         const int d = s + t + 2;  // 1-based pair sum
-        const bool top = d <= kTopD;
+        const bool top = d <= kTopDL;
         if (tid == 0) {
           mbar_expect_tx(bar_b, (uint32_t)(ks * kBoxB));
           for (int u = 0; u < ks; ++u)
@@ -288,7 +304,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         if (top) {
           // exact integer partial sums: I = v 2^(7d), |I| < 2^22
           const float scale = __int_as_float((127 + kBeta * d) << 23);
-          const int sh = kBeta * (kTopD - d);
+          const int sh = kBeta * (kTopDL - d);
 #pragma unroll
           for (int q = 0; q < kBN / 16; ++q) {
             uint32_t r[16];
@@ -331,7 +347,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         if (ea == kExpBad || eb == kExpBad) {
           v = __longlong_as_double(0x7FF8000000000000ll);
         } else {
-          const double top = (double)F[q * 16 + j] * 0x1p-42;  // LSB 2^(-7 kTopD)
+          const double top = (double)F[q * 16 + j] * 0x1p-49;  // LSB 2^(-7 kTopDL)
           v = scalbn(top + (double)__uint_as_float(r[j]), ea + eb);
         }
         v *= p.alpha;
@@ -434,7 +450,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       for (int c = 0; c < nchunk && ok; ++c) {
         const int k0 = c * kChunk;
         const int ks = min(kBoxes, (p.kp - k0) / kKStep);
-        for (int s = 0; s < kSlices && ok; ++s) {
+        for (int s = 0; s < kSlicesL && ok; ++s) {
           const int as = ja & 1, ka = ja >> 1;
           if (!(ok = mbar_wait_ab(bar(BA_EMPTY + as), (ka & 1) ^ 1, abort))) break;
           mbar_expect_tx(bar(BA_FULL + as), (uint32_t)(ks * kBoxA));
@@ -443,7 +459,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
           last_a = bar(BA_FULL + as);
           last_a_ph = ka & 1;
           ++ja;
-          for (int t = 0; s + t <= kSlices - 1; ++t) {
+          for (int t = 0; s + t <= kSlicesL - 1; ++t) {
             const int bs = jb & 1, kb = jb >> 1;
             if (!(ok = mbar_wait_ab(bar(BB_EMPTY + bs), (kb & 1) ^ 1, abort))) break;
             mbar_expect_tx(bar(BB_FULL + bs), (uint32_t)(ks * kBoxB));
@@ -471,12 +487,12 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       for (int c = 0; c < nchunk && ok; ++c) {
         const int k0 = c * kChunk;
         const int ks = min(kBoxes, (p.kp - k0) / kKStep);
-        for (int s = 0; s < kSlices && ok; ++s) {
+        for (int s = 0; s < kSlicesL && ok; ++s) {
           const int as = ja & 1, ka = ja >> 1;
           if (!(ok = mbar_wait_ab(bar(BA_FULL + as), ka & 1, abort))) break;
-          for (int t = 0; s + t <= kSlices - 1; ++t) {
+          for (int t = 0; s + t <= kSlicesL - 1; ++t) {
             const int d = s + t + 2;
-            const bool top = d <= kTopD;
+            const bool top = d <= kTopDL;
             const int bs = jb & 1, kb = jb >> 1;
             if (!(ok = mbar_wait_ab(bar(BB_FULL + bs), kb & 1, abort))) break;
             const int slot = jt & 1, kt = jt >> 1;
@@ -498,7 +514,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
               mma_commit(bar(BACC_FULL + slot));
               ++jt;
             }
-            if (s + t == kSlices - 1) mma_commit(bar(BA_EMPTY + as));
+            if (s + t == kSlicesL - 1) mma_commit(bar(BA_EMPTY + as));
             ++jb;
           }
           ++ja;
@@ -517,16 +533,16 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
     int jt = 0;
     bool ok = true;
     for (int c = 0; c < nchunk && ok; ++c) {
-      for (int s = 0; s < kSlices && ok; ++s) {
-        for (int t = 0; s + t <= kSlices - 1 && ok; ++t) {
+      for (int s = 0; s < kSlicesL && ok; ++s) {
+        for (int t = 0; s + t <= kSlicesL - 1 && ok; ++t) {
           const int d = s + t + 2;
-          if (d > kTopD) continue;
+          if (d > kTopDL) continue;
           const int slot = jt & 1, kt = jt >> 1;
           ok = __all_sync(0xffffffffu, mbar_wait_ab(bar(BACC_FULL + slot), kt & 1, abort));
           if (!ok) break;
           tc_fence_after();
           const float scale = __int_as_float((127 + kBeta * d) << 23);
-          const int sh = kBeta * (kTopD - d);
+          const int sh = kBeta * (kTopDL - d);
 #pragma unroll
           for (int q = 0; q < kBN / 16; ++q) {
             uint32_t r[16];
@@ -567,7 +583,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
           if (ea == kExpBad || eb == kExpBad) {
             v = __longlong_as_double(0x7FF8000000000000ll);
           } else {
-            const double top = (double)F[q * 16 + j] * 0x1p-42;  // LSB 2^(-7 kTopD)
+            const double top = (double)F[q * 16 + j] * 0x1p-49;  // LSB 2^(-7 kTopDL)
             v = scalbn(top + (double)__uint_as_float(r[j]), ea + eb);
           }
           v *= p.alpha;
@@ -613,13 +629,13 @@ void load_encode() {
 inline size_t r256(size_t x) { return (x + 255) & ~(size_t)255; }
 inline int kpad(int k) { return ((2 * k + kKStep - 1) / kKStep) * kKStep; }
 
-// 4-D map over slices [nb][kSlices][rows][kp] (BF16) with a box of
+// 4-D map over slices [nb][kSlicesL][rows][kp] (BF16) with a box of
 // kKStep x box_rows x 1 x 1 and 128-byte swizzling; rows beyond `rows`
 // read as zeros
 bool encode_slices(CUtensorMap* map, void* base, int kp, int rows, int nb, int box_rows) {
-  const cuuint64_t dims[4] = {(cuuint64_t)kp, (cuuint64_t)rows, (cuuint64_t)kSlices, (cuuint64_t)nb};
+  const cuuint64_t dims[4] = {(cuuint64_t)kp, (cuuint64_t)rows, (cuuint64_t)kSlicesL, (cuuint64_t)nb};
   const cuuint64_t strides[3] = {(cuuint64_t)kp * 2, (cuuint64_t)kp * 2 * rows,
-                                 (cuuint64_t)kp * 2 * rows * kSlices};
+                                 (cuuint64_t)kp * 2 * rows * kSlicesL};
   const cuuint32_t box[4] = {(cuuint32_t)kKStep, (cuuint32_t)box_rows, 1, 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   return g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, base, dims, strides, box, estr,
@@ -638,8 +654,8 @@ Carve carve(char* base, int m, int n, int k, int nba, int nbb) {
   const int kp = kpad(k);
   Carve c;
   size_t off = 0;
-  const size_t a_b = r256((size_t)nba * kSlices * 2 * m * kp * 2);
-  const size_t b_b = r256((size_t)nbb * kSlices * n * kp * 2);
+  const size_t a_b = r256((size_t)nba * kSlicesL * 2 * m * kp * 2);
+  const size_t b_b = r256((size_t)nbb * kSlicesL * n * kp * 2);
   c.sa = reinterpret_cast<uint16_t*>(base ? base + off : nullptr);
   off += a_b;
   c.sb = reinterpret_cast<uint16_t*>(base ? base + off : nullptr);
@@ -679,7 +695,7 @@ size_t zgemm_workspace(int m, int n, int k, int batch, bool a_shared, bool b_sha
 
 cudaError_t zgemm(const ZgemmArgs& g, void* work, size_t work_bytes, int* err, cudaStream_t st) {
   if (g.m <= 0 || g.n <= 0 || g.batch <= 0) return cudaSuccess;
-  if (g.k <= 0) return cudaErrorInvalidValue;
+  if (g.k <= 0 || g.k > kMaxK) return cudaErrorInvalidValue;
   if (!tma_available()) return cudaErrorNotSupported;
   const bool ash = g.sA == 0, bsh = g.sB == 0;
   const int nba = ash ? 1 : g.batch, nbb = bsh ? 1 : g.batch;
@@ -767,6 +783,7 @@ int pf_tc_zgemm_dev(int transa, int transb, int m, int n, int k, double alpha, c
     return tc_set_err(PF_ERR_ARG, "pf_tc_zgemm: trans must be 'N' or 'C'");
   if (m == 0 || n == 0 || batch == 0) return PF_SUCCESS;
   if (k == 0) return tc_set_err(PF_ERR_ARG, "pf_tc_zgemm: k must be positive");
+  if (k > pf::tc::kMaxK) return tc_set_err(PF_ERR_SIZE, "pf_tc_zgemm: k above 2048");
   if (!A || !B || !C || !work) return tc_set_err(PF_ERR_ARG, "pf_tc_zgemm: null pointer");
   const int rowsA = transa == 'N' ? m : k, rowsB = transb == 'N' ? k : n;
   if (lda < rowsA || ldb < rowsB || ldc < m) return tc_set_err(PF_ERR_ARG, "pf_tc_zgemm: leading dimension too small");

@@ -23,12 +23,14 @@ namespace tc {
 // about 2^-40 of the accumulator (measured), so only pairs that light may
 // share the inexact accumulator.
 constexpr int kBeta = 7;
-constexpr int kSlices = 8;
+constexpr int kSlices = 8;   // the 32-wide CTA-level products (tc_small.cuh)
+constexpr int kSlicesL = 9;  // the batched large products (tc_abi.cu): 63-bit fixed point
 constexpr int kTopD = 6;
 constexpr int kBM = 128;     // rows of the real product per CTA (TMEM lanes)
 constexpr int kBN = 64;      // columns per CTA
 constexpr int kKStep = 64;   // K per TMA box (one 128-byte swizzle row of BF16)
 constexpr int kChunk = 256;  // K per exact accumulation chain: 127^2 * 256 < 2^22
+constexpr int kMaxK = 2048;  // largest complex K of the large products (16 chunks of the real K)
 
 struct ZgemmArgs {
   int m, n, k;                 // op(A) is m x k, op(B) is k x n (complex)

@@ -71,11 +71,34 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+}
+
+// The same load without the wait: several loads are issued back to back and
+// completed by one tmem_wait_ld() before any of their registers is used.
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
       "%15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
         "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      : "r"(taddr)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// Ties registers filled by tmem_ld16_nowait to a point after tmem_wait_ld():
+// the compiler sees them redefined here (volatile asm statements keep their
+// order), so no use of them moves above the wait.
+__device__ __forceinline__ void tmem_regs_ready(uint32_t (&r)[16]) {
+  asm volatile(""
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15]));
 }
 
 __device__ __forceinline__ unsigned long long mag_bits(double v) {
@@ -90,9 +113,11 @@ __device__ __forceinline__ int exp_of_maxbits(unsigned long long m) {
   return ef == 0 ? -1022 : ef - 1022;
 }
 
-// 56-bit truncated fixed point of x = a 2^-e (|x| < 1), from the FP64 bits
-// (integer operations only); the sign is returned separately.
-__device__ __forceinline__ unsigned long long fixed56(double a, int e, bool& neg) {
+// Bits-bit truncated fixed point of x = a 2^-e (|x| < 1), from the FP64
+// bits (integer operations only); the sign is returned separately.
+template <int Bits>
+__device__ __forceinline__ unsigned long long fixed_pt(double a, int e, bool& neg) {
+  static_assert(Bits >= 53 && Bits <= 63, "one 64-bit word");
   const unsigned long long bits = (unsigned long long)__double_as_longlong(a);
   neg = (bits >> 63) != 0;
   const int ef = (int)((bits >> 52) & 0x7FF);
@@ -100,19 +125,26 @@ __device__ __forceinline__ unsigned long long fixed56(double a, int e, bool& neg
   if (ef != 0) mant |= 0x0010000000000000ull;
   if (mant == 0 || e == kExpBad || ef == 0x7FF) return 0;
   const int eeff = ef == 0 ? 1 : ef;
-  // a = mant 2^(eeff - 1075); x 2^56 = mant 2^(eeff - 1019 - e)
-  const int sh = eeff - 1019 - e;
-  if (sh >= 0) return sh >= 4 ? 0 : (mant << sh);  // sh <= 3 whenever |x| < 1
+  // a = mant 2^(eeff - 1075); x 2^Bits = mant 2^(eeff - 1075 + Bits - e)
+  const int sh = eeff - (1075 - Bits) - e;
+  if (sh >= 0) return sh > Bits - 53 ? 0 : (mant << sh);  // sh <= Bits - 53 whenever |x| < 1
   return sh <= -64 ? 0 : (mant >> (-sh));
 }
-// BF16 bits of q 2^-(7s), q the s-th 7-bit group of F
-__device__ __forceinline__ uint16_t slice_bf16(unsigned long long F, int s, bool neg) {
-  const int q = (int)((F >> (kBeta * (kSlices - s))) & 127u);
+__device__ __forceinline__ unsigned long long fixed56(double a, int e, bool& neg) { return fixed_pt<56>(a, e, neg); }
+
+// BF16 bits of q 2^-(7s), q the s-th 7-bit group (from the top) of the
+// (7 Slices)-bit fixed point F
+template <int Slices>
+__device__ __forceinline__ uint16_t slice_bf16_n(unsigned long long F, int s, bool neg) {
+  const int q = (int)((F >> (kBeta * (Slices - s))) & 127u);
   if (q == 0) return 0;
   // q as a float (exact), scaled by 2^-(7s) through the exponent field
   const float f = __int_as_float(0x4B000000 | q) - 8388608.0f;
   const unsigned int fb = (unsigned int)__float_as_int(f) - ((unsigned int)(kBeta * s) << 23);
   return (uint16_t)((fb >> 16) | (neg ? 0x8000u : 0u));
+}
+__device__ __forceinline__ uint16_t slice_bf16(unsigned long long F, int s, bool neg) {
+  return slice_bf16_n<kSlices>(F, s, neg);
 }
 
 

@@ -211,6 +211,61 @@ def transport_tdb_modes(E, blocks, geometry, ksc, *, eta, eta0, convergence, lam
     return out
 
 
+BLOCK_OUTPUTS = ("gl_adv", "gl_plus", "gr_ret", "gr_minus", "gml_adv", "gmr_ret", "G_D_LR", "G_R", "G_D_RL", "G_L")
+
+
+def transport_tdb_blocks(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=None, zero_flag=None,
+                         max_iter=1000, want=BLOCK_OUTPUTS, check=True):
+    """FP64 transmission plus the Green's-function blocks that vel_mat_tdb
+    receives (pf_transport_tdb_blocks_dev): the surface functions gl_adv,
+    gl_plus, gr_ret, gr_minus, the broadenings gml_adv, gmr_ret, and
+    G_D_LR = G_{0,N+1}, G_R, G_D_RL = G_{N+1,0}, G_L.  ``want`` names the
+    blocks to return (complex (npts, rows, cols) arrays); the others are not
+    written on the device.  Also returns transl, transr and status."""
+    import torch
+    lib = _abi.load()
+    if isinstance(blocks, dict):
+        blocks = TdbBlocks.from_dict(blocks)
+    nq, (n, nl, nr, L), arrs = blocks.stacked()
+    unknown = set(want) - set(BLOCK_OUTPUTS)
+    if unknown:
+        raise ValueError(f"unknown blocks {sorted(unknown)}")
+    dev = {k: torch.from_numpy(fortran_block(v).copy()).cuda() for k, v in arrs.items()}
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    npts = E.size
+    Ed = torch.from_numpy(E).cuda()
+    qd = None if qidx is None else torch.from_numpy(np.ascontiguousarray(qidx, dtype=np.int32)).cuda()
+    zd = None if zero_flag is None else torch.from_numpy(np.ascontiguousarray(zero_flag, dtype=np.int32)).cuda()
+    tl = torch.zeros(max(npts, 1), dtype=torch.float64, device="cuda")
+    tr = torch.zeros_like(tl)
+    st = torch.zeros(max(npts, 1), dtype=torch.int32, device="cuda")
+    shapes = dict(gl_adv=(nl, nl), gl_plus=(nl, nl), gr_ret=(nr, nr), gr_minus=(nr, nr), gml_adv=(nl, nl),
+                  gmr_ret=(nr, nr), G_D_LR=(nl, nr), G_R=(nr, nr), G_D_RL=(nr, nl), G_L=(nl, nl))
+    bufs = {k: torch.zeros((max(npts, 1), shapes[k][1], shapes[k][0], 2), dtype=torch.float64, device="cuda")
+            for k in want}
+    ws = lib.pf_transport_tdb_blocks_workspace_size(n, nl, nr, nq, npts)
+    if ws == 0:
+        raise _abi.PFError(-3, "kernel does not fit (block size > 48?)")
+    work = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    p = lambda t: None if t is None else t.data_ptr()
+    rc = lib.pf_transport_tdb_blocks_dev(n, nl, nr, L, nq, *[dev[k].data_ptr() for k in BLOCK_NAMES], npts,
+                                         Ed.data_ptr(), p(qd), p(zd), eta, eta0, dev_factor, convergence, max_iter,
+                                         tl.data_ptr(), tr.data_ptr(), st.data_ptr(),
+                                         *[p(bufs.get(k)) for k in BLOCK_OUTPUTS], work.data_ptr(), ws,
+                                         C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if rc != 0:
+        raise _abi.PFError(rc, lib.pf_modes_last_error().decode(errors="replace"))
+    torch.cuda.synchronize()
+    status = st.cpu().numpy()[:npts]
+    if check and (status != 0).any():
+        raise _abi.PFError(-4, f"point status flags 0x{int(np.bitwise_or.reduce(status)):x}")
+    out = dict(transl=tl.cpu().numpy()[:npts], transr=tr.cpu().numpy()[:npts], status=status)
+    for k, v in bufs.items():
+        a = v.cpu().numpy()[:npts]                      # (npts, cols, rows, 2): column-major blocks
+        out[k] = np.transpose(a[..., 0] + 1j * a[..., 1], (0, 2, 1))
+    return out
+
+
 KINDS = ("adv_l", "ret_l", "ret_r", "adv_r")
 MATRICES = ("tlr", "trl", "rrr", "rll")
 # write_specular calls (velocity_mat.f90:3108-3120): file -> (matrix, incoming problem)

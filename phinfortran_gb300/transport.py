@@ -134,9 +134,10 @@ def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=No
     qidx: (npts,) q index into the stacked blocks (None: all 0).
     zero_flag: (npts,) nonzero -> T forced to 0 (the reference's ie == 1).
     precision: "fp64" (pf_transport_tdb) or "mixed" (pf_transport_tdb_mixed:
-    double-float leads, FP32 factorisation, double-float refinement: one
-    sweep for every point and up to `refine_iters` - 1 more for the points
-    whose last correction of G_{0,N+1} was above 3e-5 relative; T_L only).
+    FP64-grade lead decimations with their block products on the tensor
+    cores, FP32 factorisation, double-float refinement: one sweep for every
+    point and up to `refine_iters` - 1 more for the points whose last
+    correction of G_{0,N+1} was above 3e-5 relative; T_L only).
     Blocks above 48 go through the large-block entry, where "mixed" (or
     "tc") puts the block products on the tensor cores and "df64" selects
     the double-float engine.
