@@ -120,13 +120,15 @@ int pf_transport_tdb(int n, int nl, int nr, int L, int nq,
 /*
  * Mixed-precision transport (T_L only), device pointers.  Same inputs and
  * meaning as pf_transport_tdb_dev; the arithmetic differs:
- *   - both lead decimations (negf/surface.f90:488-497) run in FP64: the
- *     doubling iteration amplifies its own rounding, and near subband edges
- *     at eta ~ 1e-6 double-float (48-bit) decimations leave T up to 5e-8
- *     away from FP64 even where FP64 itself is reproducible;
- *     pf_transport_tdb_mixed_ex_dev selects double-float decimations
- *     (pairs of FP32 numbers on the FP32 pipe) or split ones (first 8 steps
- *     FP64, the rest double-float) for speed;
+ *   - the lead decimations (negf/surface.f90:488-497) for blocks up to 32
+ *     run in FP64 arithmetic with their block products on the tensor cores
+ *     (exact BF16 slice products): the doubling iteration amplifies its
+ *     own rounding, and near subband edges at eta ~ 1e-6 double-float
+ *     (48-bit) decimations leave T up to 5e-8 away from FP64 even where
+ *     FP64 itself is reproducible.  Above 32 they run in double-float
+ *     (pairs of FP32 numbers on the FP32 pipe): there FP64 decimations have
+ *     no tensor-core path and cost twice the whole double-float solve
+ *     (PF_ARITH_AUTO; pf_transport_tdb_mixed_ex_dev chooses explicitly);
  *   - the device blocks are factorised in FP32 (the left-connected
  *     recursion of negf/lesser.f90:547-654 as a block LU of the extended
  *     lead+device matrix), and the last block column G_{:,N+1} is refined
@@ -135,8 +137,7 @@ int pf_transport_tdb(int n, int nl, int nr, int L, int nq,
  *     block X_0 = G_{0,N+1} was above 3e-5 (PF_REFINE_TOL) relative to X_0 (refine_iters
  *     in [0, 16]; 0 keeps the FP32 solution);
  *   - the Caroli trace (negf/lesser.f90:787-792) is taken in double-float.
- * The per-point matrix work uses no FP64 arithmetic.  work must hold
- * pf_transport_tdb_mixed_workspace_size(...) bytes.
+ * work must hold pf_transport_tdb_mixed_workspace_size(...) bytes.
  */
 size_t pf_transport_tdb_mixed_workspace_size(int n, int nl, int nr, int L,
                                              int nq, int npts);
@@ -156,12 +157,15 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq,
 
 /*
  * pf_transport_tdb_mixed_dev with the lead arithmetic chosen by lead_arith:
- * PF_ARITH_FP64 (whole decimations in FP64: what pf_transport_tdb_mixed_dev
- * does), PF_ARITH_SPLIT (the first 8 decimation steps in FP64, the rest in
+ * PF_ARITH_AUTO (what pf_transport_tdb_mixed_dev does: PF_ARITH_FP64 for
+ * blocks up to 32, PF_ARITH_DF64 above), PF_ARITH_FP64 (whole decimations
+ * in FP64; block products on the tensor cores up to 32, FP64 SIMT above),
+ * PF_ARITH_SPLIT (the first 8 decimation steps in FP64, the rest in
  * double-float) or PF_ARITH_DF64 (whole decimations in double-float).  Same
  * workspace size.
  */
 #define PF_ARITH_SPLIT 3
+#define PF_ARITH_AUTO (-1)
 int pf_transport_tdb_mixed_ex_dev(int n, int nl, int nr, int L, int nq,
                                   const double* HL, const double* HLv,
                                   const double* HR, const double* HRv,
@@ -468,6 +472,20 @@ int pf_transport_tdb_blocks_dev(int n, int nl, int nr, int L, int nq,
                                 double* G_D_LR, double* G_R, double* G_D_RL,
                                 double* G_L, void* work, size_t work_bytes,
                                 void* stream);
+
+/*
+ * Stage timing of the mixed pipeline (blocks up to 32).  No reference
+ * counterpart (profiling aid).  After pf_mixed_stage_timing(1) every mixed
+ * call records CUDA events on its stream; pf_mixed_stage_times(ms, n >= 3)
+ * waits for the last call's events and writes the durations in ms of
+ * (0) the block conversions and sparse copies, (1) the lead decimations
+ * (one kernel), (2) the factorisation, refinement and Caroli sweeps, and
+ * returns 3 (or a negative error code; message in pf_last_error).  Off by
+ * default; timed calls must not overlap and must not be captured into a
+ * CUDA graph.
+ */
+int pf_mixed_stage_timing(int on);
+int pf_mixed_stage_times(float* ms, int n);
 
 /* Message for the last error of the mode-resolved entry points. */
 const char* pf_modes_last_error(void);

@@ -19,10 +19,8 @@ LIB = os.path.join(OUT_DIR, "libphinfortran_gb300.so")
 
 SOURCES = ["negf_abi.cu", "dyn_abi.cu", "cond_abi.cu", "grad_abi.cu", "grad_fp64.cu", "grad_df64.cu", "modes_abi.cu", "tiled_abi.cu", "tb_abi.cu", "fullh_abi.cu", "probe_abi.cu", "tc_abi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# --split-compile runs the device optimiser of one translation unit on several
-# threads (the largest unit, negf_abi.cu, otherwise takes minutes alone)
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "--split-compile=0", "-I", os.path.join(ROOT, "include")]
+              "-I", os.path.join(ROOT, "include")]
 
 
 def nvcc():

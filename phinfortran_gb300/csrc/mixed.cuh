@@ -206,6 +206,55 @@ __device__ void copy_cvt(cx<A>* dst, int ldd, bool conj_t, const cx<B>* src, int
 // restored by one gather, inv(k, P(j)) = A(P(k), j).  fbuf holds two
 // buffers of m multipliers (the pivot row's entry carries 1 / pivot); the
 // status bits (PF_SINGULAR, PF_NAN) are those of inverse().
+// Helpers of the tensor-core decimation that keep work off the FP64 pipe.
+// W = z - e: the negation as a flip of the sign bit (integer operation),
+// one FP64 addition on the diagonal.
+__device__ void shift_neg_bits(cx<double>* dst, int ldd, cx<double> z, const cx<double>* src, int lds, int n) {
+  for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+    const int r = i % n, c = i / n;
+    const cx<double> v = src[r + c * lds];
+    cx<double> w = mk<double>(__longlong_as_double(__double_as_longlong(v.x) ^ (long long)0x8000000000000000ull),
+                              __longlong_as_double(__double_as_longlong(v.y) ^ (long long)0x8000000000000000ull));
+    if (r == c) w = mk<double>(z.x - v.x, z.y - v.y);
+    dst[r + c * ldd] = w;
+  }
+  __syncthreads();
+}
+
+// max_ij |a_ij| for the stopping test, as the square root of the largest
+// re^2 + im^2 (two FP64 operations an entry instead of hypot's scaled
+// evaluation; equal to a few ulps, so the stopping step can differ from the
+// FP64 path's only when the test value sits within rounding of the
+// threshold).  NaN propagates.
+__device__ double max_mod_sq(const cx<double>* a, int ld, int m, double* red) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < m * m; i += blockDim.x) {
+    const cx<double> e = a[i % m + (i / m) * ld];
+    const double h = fma(e.x, e.x, e.y * e.y);
+    v = (h > v || h != h) ? h : v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = (w > v || w != w) ? w : v;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      const double w = __shfl_xor_sync(0xffffffffu, v, o);
+      v = (w > v || w != w) ? w : v;
+    }
+    if (lane == 0) red[0] = sqrt(v);
+  }
+  __syncthreads();
+  v = red[0];
+  __syncthreads();
+  return v;
+}
+
 struct LaWork {
   cx<double>* f;  // [2 m]
   int* perm;      // [n]
@@ -344,14 +393,14 @@ __device__ int decimate_tc(const Ctx<double>& c, tc::SmallTC& t, int m, cx<doubl
   copy_in(es, ld, h00, m, m);
   copy_in(al, ld, a0, m, m);
   copy_in(be, ld, b0, m, m);
-  double maxdiff = max_abs(al, ld, m, m, c.red);
+  double maxdiff = max_mod_sq(al, ld, m, c.red);
   int it = 0;
   while (maxdiff > conv) {
     if (it >= max_iter) {
       st |= PF_NOT_CONVERGED;
       break;
     }
-    shift_neg(W1, ld, z, e1, ld, m);                                                 // z - e1
+    shift_neg_bits(W1, ld, z, e1, ld, m);                                                 // z - e1
     st |= inverse_la(W1, c.sm[3], ld, m, la);                                        // ive
     // the six products of a step as two tensor-core calls:
     //   [W2; W3] = [alpha; beta] ive, then
@@ -384,11 +433,11 @@ __device__ int decimate_tc(const Ctx<double>& c, tc::SmallTC& t, int m, cx<doubl
       e.y += w.y;
     }
     __syncthreads();
-    maxdiff = max_abs(al, ld, m, m, c.red);
+    maxdiff = max_mod_sq(al, ld, m, c.red);
     ++it;
   }
   if (maxdiff != maxdiff) st |= PF_NAN;
-  shift_neg(W1, ld, z, es, ld, m);
+  shift_neg_bits(W1, ld, z, es, ld, m);
   st |= inverse_la(W1, c.sm[3], ld, m, la);
   if (iters_out) *iters_out = it;
   return st;

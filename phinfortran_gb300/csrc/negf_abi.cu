@@ -1390,6 +1390,28 @@ size_t pf_transport_tdb_mixed_workspace_size(int n, int nl, int nr, int L, int n
 namespace {
 // One pass of the mixed pipeline over npts points with the workspace `work`
 // laid out by `plan` (made for at least npts points), on stream st.
+// Optional stage timing of the mixed pipeline (pf_mixed_stage_timing):
+// events recorded on the call's stream before the block conversions, around
+// the lead decimations and after the last sweep.  One set per process; the
+// calls being timed must not overlap and must not be captured into a graph.
+struct StageTimer {
+  bool on = false;
+  bool ready = false;
+  bool recorded = false;
+  cudaEvent_t ev[4];
+  void mark(int i, cudaStream_t st) {
+    if (!on) return;
+    if (!ready) {
+      for (auto& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+      ready = true;
+    }
+    cudaEventRecord(ev[i], st);
+    if (i == 3) recorded = true;
+  }
+};
+StageTimer g_timer;
+
 int mixed_launch(const MixedPlan& plan, int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
                  const double* HR, const double* HRv, const double* Hd, const double* Hdv, const double* Hld,
                  const double* Hrd, int npts, const double* E, const int* qidx, const int* zero_flag, double eta,
@@ -1426,6 +1448,7 @@ int mixed_launch(const MixedPlan& plan, int n, int nl, int nr, int L, int nq, co
   }
   int* mirror = reinterpret_cast<int*>(p);
   char* scratch = w + plan.off_scratch;
+  g_timer.mark(0, st);
   for (int i = 0; i < 8; ++i) {
     if (lay.cnt[i] == 0) continue;
     const int blocks = (int)((lay.cnt[i] + 255) / 256 < 4096 ? (lay.cnt[i] + 255) / 256 : 4096);
@@ -1520,12 +1543,15 @@ int mixed_launch(const MixedPlan& plan, int n, int nl, int nr, int L, int nq, co
       if (gs_smem) smem_tc += gs_bytes;
       PF_CUDA(cudaFuncSetAttribute(leads_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tc));
       const int grid_tc = plan.grid_a < di.sms ? plan.grid_a : di.sms;
+      g_timer.mark(1, st);
       leads_tc_kernel<<<grid_tc, kThreads, smem_tc, st>>>(sys, pts, P, out, lay, plan.per_cta_a, scratch, lo, lstat,
                                                           queue, gs_smem);
     } else {
+      g_timer.mark(1, st);
       leads_kernel<1><<<plan.grid_a, kThreads, lay.smem_leads, st>>>(sys, pts, P, out, lay, plan.per_cta_a, scratch,
                                                                       lo, lstat, queue);
     }
+    g_timer.mark(2, st);
     PF_CUDA(cudaGetLastError());
     // factorisation + back substitution, then each refinement sweep as a
     // parallel residual kernel followed by the warp-per-point correction,
@@ -1563,6 +1589,7 @@ int mixed_launch(const MixedPlan& plan, int n, int nl, int nr, int L, int nq, co
     PF_CUDA(cudaMemsetAsync(queue_b, 0, sizeof(int), st));
     layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 2, out, lo, sl, lstat, queue_b,
                                                                        nullptr, nullptr);
+    g_timer.mark(3, st);
   } else if (S == 1) {
     mixed_kernel<1><<<plan.grid_a, kMixedThreads, lay.smem, st>>>(sys, pts, P, refine_iters, out, lay, scratch, queue);
   } else {
@@ -1579,13 +1606,18 @@ int mixed_ex(int n, int nl, int nr, int L, int nq, const double* HL, const doubl
              int* iters, void* work, size_t work_bytes, void* stream) {
   int rc = check_dims(n, nl, nr, L, nq, npts);
   if (rc != PF_SUCCESS) return rc;
+  if (lead_arith == PF_ARITH_AUTO) {
+    // FP64 decimations where their block products run on the tensor cores
+    const int mx = nl > nr ? nl : nr;
+    lead_arith = mx <= pf::tc::kSmallN && n <= pf::wp::NW ? PF_ARITH_FP64 : PF_ARITH_DF64;
+  }
+  if (lead_arith != PF_ARITH_FP64 && lead_arith != PF_ARITH_DF64 && lead_arith != PF_ARITH_SPLIT)
+    return set_err(PF_ERR_ARG, "pf: lead_arith must be PF_ARITH_AUTO, PF_ARITH_FP64, PF_ARITH_DF64 or PF_ARITH_SPLIT");
   if (!E || !transl || !status) return set_err(PF_ERR_ARG, "pf: null energy/output pointer");
   if (!HL || !HLv || !HR || !HRv || !Hd || !Hld || !Hrd || (L > 1 && !Hdv))
     return set_err(PF_ERR_ARG, "pf: null block pointer");
   if (max_iter <= 0 || refine_iters < 0 || refine_iters > 16)
     return set_err(PF_ERR_ARG, "pf: max_iter must be positive and refine_iters in [0, 16]");
-  if (lead_arith != PF_ARITH_FP64 && lead_arith != PF_ARITH_DF64 && lead_arith != PF_ARITH_SPLIT)
-    return set_err(PF_ERR_ARG, "pf: lead_arith must be PF_ARITH_FP64, PF_ARITH_DF64 or PF_ARITH_SPLIT");
   if (npts == 0) return PF_SUCCESS;
   const int lead_mode = lead_arith == PF_ARITH_FP64 ? pf::PF_LEAD_FP64
                                                     : (lead_arith == PF_ARITH_DF64 ? pf::PF_LEAD_DF64 : pf::PF_LEAD_SPLIT);
@@ -1601,6 +1633,21 @@ int mixed_ex(int n, int nl, int nr, int L, int nq, const double* HL, const doubl
 }  // namespace
 
 extern "C" {
+int pf_mixed_stage_timing(int on) {
+  g_timer.on = on != 0;
+  g_timer.recorded = false;
+  return PF_SUCCESS;
+}
+
+int pf_mixed_stage_times(float* ms, int n) {
+  if (!ms || n < 3) return set_err(PF_ERR_ARG, "pf_mixed_stage_times: need room for three durations");
+  if (!g_timer.ready || !g_timer.recorded)
+    return set_err(PF_ERR_ARG, "pf_mixed_stage_times: no timed call of the 32-wide pipeline");
+  PF_CUDA(cudaEventSynchronize(g_timer.ev[3]));
+  for (int i = 0; i < 3; ++i) PF_CUDA(cudaEventElapsedTime(&ms[i], g_timer.ev[i], g_timer.ev[i + 1]));
+  return 3;
+}
+
 int pf_transport_tdb_mixed_ex_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
                                   const double* HR, const double* HRv, const double* Hd, const double* Hdv,
                                   const double* Hld, const double* Hrd, int npts, const double* E, const int* qidx,
@@ -1620,7 +1667,7 @@ int pf_transport_tdb_mixed_dev(int n, int nl, int nr, int L, int nq, const doubl
                                double convergence, int max_iter, int refine_iters, double* transl, int* status,
                                int* iters, void* work, size_t work_bytes, void* stream) {
   return mixed_ex(n, nl, nr, L, nq, HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd, npts, E, qidx, zero_flag, eta, eta0,
-                  dev_factor, convergence, max_iter, refine_iters, PF_ARITH_FP64, transl, status, iters, work,
+                  dev_factor, convergence, max_iter, refine_iters, PF_ARITH_AUTO, transl, status, iters, work,
                   work_bytes, stream);
 }
 

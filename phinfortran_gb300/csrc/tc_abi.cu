@@ -14,9 +14,8 @@
 //     truncated to a 63-bit integer F (integer operations on the FP64 bits);
 //   * slice s = 1..9 holds q_s * 2^-7s with q_s the s-th 7-bit group of F
 //     (|q_s| <= 127: exact in BF16), so x = sum_s q_s 2^-7s + O(2^-63).
-//     An entry 2^-10 below the largest of its row still keeps all 53 bits;
-//     with eight slices (56 bits) the blocks of a wide multi-orbital ribbon,
-//     whose rows span several decades, gave T 2e-7 away from FP64;
+//     An entry 2^-10 below the largest of its row still keeps all 53 bits
+//     (the blocks of a wide multi-orbital ribbon span several decades);
 //   * the product keeps the slice pairs with s + t <= 10.  For s + t <= 7 the
 //     FP32 tensor-core sums over K chunks of 256 are integers below 2^22
 //     (127^2 * 256 < 2^22), hence exact; each chunk is drained from TMEM and

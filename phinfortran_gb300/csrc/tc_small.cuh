@@ -137,10 +137,26 @@ __device__ __forceinline__ void small_wait(SmallTC& t, int b) {
   if (!ok) *t.abort = 1;
 }
 
-// 2^e as a double for e in the normal range, 0 outside it (the caller then
-// falls back to scalbn)
-__device__ __forceinline__ double small_pow2(int e) {
-  return (e >= -1022 && e <= 1023) ? __longlong_as_double((long long)(e + 1023) << 52) : 0.0;
+// F 2^s + lo 2^t as a double, rounded once, with two FP64 additions (the
+// FP64 pipe is the narrow one on this part): F (|F| < 2^51) is scaled
+// exactly by the magic-number form -- the bits of M = 1.5 2^(52+s) plus F
+// are the double M + F 2^s, and subtracting M is exact -- and lo (FP32) is
+// widened with its exponent moved by t through integer operations.  Out of
+// the normal range (or lo subnormal) the plain conversions are used.
+__device__ __forceinline__ double small_assemble(long long F, float lo, int s, int t) {
+  const unsigned int lb = __float_as_uint(lo);
+  const int le = (int)((lb >> 23) & 0xFF);
+  const bool lo_zero = (lb & 0x7FFFFFFFu) == 0u;
+  const int de = le - 127 + t + 1023;  // biased double exponent of lo 2^t
+  if (s < -1070 || s > 960 || (!lo_zero && (le == 0 || de < 1 || de > 2046)))
+    return scalbn((double)F, s) + scalbn((double)lo, t);
+  const long long mb = ((long long)(1023 + 52 + s) << 52) | (1ll << 51);
+  const double M = __longlong_as_double(mb);
+  const double f = __longlong_as_double(mb + F) - M;
+  const double l = lo_zero ? 0.0
+                           : __longlong_as_double(((long long)(lb >> 31) << 63) | ((long long)de << 52) |
+                                                  ((long long)(lb & 0x7FFFFFu) << 29));
+  return f + l;
 }
 
 // C_kb = op(A_k) op(B_b) for k = 0, 1 and b < NB.  out(k, b, i, c, part,
@@ -334,11 +350,8 @@ __device__ bool small_zgemm(SmallTC& t, int m, Op<double> A0, Op<double> A1, con
           if (ea == kExpBad || eb == kExpBad) {
             v = __longlong_as_double(0x7FF8000000000000ll);
           } else {
-            // F in units of 2^-42 and the light pairs scaled to that unit
-            // (power-of-two scalings are exact; the sum rounds once)
-            const double sum = (double)F[j] + (double)(__uint_as_float(lo[j]) * 0x1p42f);
-            const double p2 = small_pow2(ea + eb - 42);
-            v = p2 != 0.0 ? sum * p2 : scalbn(sum, ea + eb - 42);
+            // F in units of 2^(ea + eb - 42), the light pairs in 2^(ea + eb)
+            v = small_assemble(F[j], __uint_as_float(lo[j]), ea + eb - 42, ea + eb);
           }
           out(k, b, i, c, part, v);
         }

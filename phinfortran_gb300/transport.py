@@ -192,7 +192,7 @@ class DeviceTransport:
 
     def __init__(self, blocks, npts_max, *, eta, eta0, convergence, dev_factor=10.0,
                  max_iter=1000, want_transr=False, device="cuda", precision="fp64", refine_iters=2,
-                 lead_arith="fp64"):
+                 lead_arith="auto"):
         import torch
         if isinstance(blocks, dict):
             blocks = TdbBlocks.from_dict(blocks)
@@ -212,7 +212,7 @@ class DeviceTransport:
         return obj
 
     def _setup(self, dev, dims, npts_max, *, eta, eta0, convergence, dev_factor=10.0, max_iter=1000,
-               want_transr=False, device="cuda", precision="fp64", refine_iters=2, lead_arith="fp64"):
+               want_transr=False, device="cuda", precision="fp64", refine_iters=2, lead_arith="auto"):
         import torch
         self.torch = torch
         lib = _abi.load()
@@ -223,11 +223,12 @@ class DeviceTransport:
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.precision = precision
         self.refine_iters = int(refine_iters)
-        # lead decimations of the mixed path: PF_ARITH_FP64 (default),
+        # lead decimations of the mixed path: PF_ARITH_AUTO (default: FP64 with
+        # tensor-core products up to 32, double-float above), PF_ARITH_FP64,
         # PF_ARITH_SPLIT (first steps FP64, the rest double-float) or PF_ARITH_DF64
-        lead_codes = {"split": 3, "fp64": 0, "df64": 1}
+        lead_codes = {"auto": -1, "split": 3, "fp64": 0, "df64": 1}
         if lead_arith not in lead_codes:
-            raise ValueError("lead_arith must be 'split', 'fp64' or 'df64'")
+            raise ValueError("lead_arith must be 'auto', 'split', 'fp64' or 'df64'")
         self.lead_arith = lead_codes[lead_arith]
         if precision == "mixed":
             want_transr = False

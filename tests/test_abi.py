@@ -79,3 +79,27 @@ def test_argument_validation_of_mode_entries_without_gpu(built_lib):
     assert rc == -1 and b"positive" in lib.pf_modes_last_error()
     rc = lib.pf_transport_tdb_modes_dev(*bad, None, 0, None)
     assert rc == -1 and b"positive" in lib.pf_modes_last_error()
+
+
+def test_argument_validation_of_tensor_core_and_mixed_entries_without_gpu(built_lib):
+    """The tensor-core GEMM refuses k above its exact-accumulation range, the
+    mixed entry unknown lead arithmetics, the blocks entry bad sizes and the
+    stage timer a query before any timed call -- all on the host."""
+    from phinfortran_gb300 import _abi
+    lib = _abi.load()
+    rc = lib.pf_tc_zgemm_dev(ord("N"), ord("N"), 4, 4, 4096, 1.0, None, 4, 0, None, 4096, 0, 0.0, None, 4, 0, 1,
+                             None, 0, None)
+    assert rc == -3 and b"2048" in lib.pf_tc_last_error()
+    rc = lib.pf_tc_zgemm_dev(ord("T"), ord("N"), 4, 4, 4, 1.0, None, 4, 0, None, 4, 0, 0.0, None, 4, 0, 1,
+                             None, 0, None)
+    assert rc == -1
+    rc = lib.pf_transport_tdb_mixed_ex_dev(4, 4, 4, 2, 1, *([None] * 8), 1, None, None, None, 0.0, 1e-6, 10.0,
+                                           1e-14, 10, 2, 7, None, None, None, None, 0, None)
+    assert rc == -1 and b"lead_arith" in lib.pf_last_error()
+    rc = lib.pf_transport_tdb_blocks_dev(0, 4, 4, 2, 1, *([None] * 8), 1, None, None, None, 0.0, 1e-6, 10.0,
+                                         1e-14, 10, None, None, None, *([None] * 10), None, 0, None)
+    assert rc == -1 and b"positive" in lib.pf_modes_last_error()
+    import ctypes as C
+    buf = (C.c_float * 3)()
+    lib.pf_mixed_stage_timing(0)
+    assert lib.pf_mixed_stage_times(buf, 3) == -1

@@ -36,6 +36,37 @@ def test_sc_bar_all_256_frequencies(cuda_ready):
     assert np.abs(r["iters"][:, 0] - o["iters_left"]).max() <= 1
 
 
+@pytest.mark.parametrize("shape", ["cfg1", "cfg4"])
+def test_mixed_sc_bar_n48(cuda_ready, shape):
+    """The mixed path on the 48-wide phonon bars (the fused kernel; the
+    default lead arithmetic is double-float there): every frequency where
+    FP64 is reproducible to 1e-10 within 1e-8 of the FP64 GPU path (cfg1:
+    all 256 frequencies of the 4 x 4 x 20 bar; cfg4: 256 of the 1024 of the
+    4 x 4 x 40 bar)."""
+    import torch
+    from phinfortran_gb300 import DeviceTransport
+    if shape == "cfg1":
+        b, E, p, _ = S.sc_phonon(ne=256)
+    else:
+        b, E, p, _ = S.sc_phonon(nx=4, ny=4, L=40, ne=1024, mass_range=(1.0, 3.0), bond_range=(0.8, 1.2),
+                                 seed_index=4)
+        E = E[::4]
+    Ed = torch.from_numpy(E).cuda()
+    T = {}
+    rng = np.random.default_rng(3)
+    bp = {k: np.asarray(v) * (1 + 1e-15 * rng.standard_normal(np.shape(v))) for k, v in b.items()}
+    for key, blocks, prec in (("fp64", b, "fp64"), ("pert", bp, "fp64"), ("mixed", b, "mixed")):
+        dt = DeviceTransport(blocks, E.size, precision=prec, **p)
+        dt.run(Ed)
+        torch.cuda.synchronize()
+        assert (dt.status[:E.size].cpu().numpy() == 0).all()
+        T[key] = dt.transl[:E.size].cpu().numpy().copy()
+    r = lambda a: np.abs(a - T["fp64"]) / np.maximum(np.abs(T["fp64"]), 1e-3)
+    good = r(T["pert"]) <= 1e-10
+    assert good.mean() > 0.9
+    assert r(T["mixed"])[good].max() <= 1e-8
+
+
 @pytest.mark.parametrize("arith", ["fp64", "df64"])
 def test_adjoint_at_full_conductance_size(cuda_ready, arith):
     """cfg4 shape: 4 x 4 x 40 bar (n = 48, L = 40), masses U[1, 3], springs

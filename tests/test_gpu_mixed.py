@@ -141,12 +141,14 @@ def test_lead_arithmetics_on_the_ribbon(cuda_ready):
     good = rel(fp.transl[:E.size].cpu().numpy(), T64) <= 1e-10
     assert good.mean() > 0.7
     out = {}
-    for lead in ("fp64", "split", "df64"):
+    for lead in ("auto", "fp64", "split", "df64"):
         dt = DeviceTransport(b, E.size, precision="mixed", lead_arith=lead, **p)
         dt.run(Ed)
         torch.cuda.synchronize()
         assert (dt.status[:E.size].cpu().numpy() == 0).all()
         out[lead] = rel(dt.transl[:E.size].cpu().numpy(), T64)
+    # blocks of 32: the default is the FP64 tensor-core decimation
+    assert np.array_equal(out["auto"], out["fp64"])
     r = out["fp64"]
     assert r[good].max() <= 1e-8, (r[good].max(), int(np.argmax(np.where(good, r, 0))))
     assert np.median(r) < 1e-9
