@@ -253,7 +253,21 @@ def large_block_sample(torch, sizes=((2, 8, 32), (3, 8, 20), (4, 2, 4))):
                         tc_max_rel_dev_from_fp64=dev["tc"], df64_max_rel_dev_from_fp64=dev["df64"],
                         status_nonzero={k: int((res[k][1]["status"] != 0).sum()) for k in res},
                         note="host-pointer call (blocks copied to the device inside the timed region); "
-                             "deviation = max |T - T64| / max(|T64|, 1e-3)"))
+                             "deviation = max |T - T64| / max(|T64|, 1e-3); built-in panel width and batch"))
+        if n == 216:
+            # the autotuner on a 48-point subsample of this problem (tensor-core
+            # arithmetic): panel width of the blocked inverse x batch
+            import tempfile
+            from phinfortran_gb300.autotune import autotune_tiled, set_tuning
+            sel = np.linspace(0, Eall.size - 1, 48).astype(int)
+            with tempfile.TemporaryDirectory() as td:
+                best = autotune_tiled(Eall[sel], b, precision="tc", panels=(8, 16, 32), batches=(16, 48),
+                                      cache=os.path.join(td, "tune.json"), qidx=q[sel], **p)
+            set_tuning(0, 0)
+            out[-1]["autotune"] = dict(sample_points=48, panel=best["panel"], batch=best["batch"],
+                                       tuned_s=best["seconds"], default_s=best["default_seconds"],
+                                       candidates=[(c["panel"], c["batch"], c["seconds"]) for c in best["candidates"]],
+                                       note="panel 0 / batch 0 = the built-in choice")
     return out
 
 

@@ -528,6 +528,18 @@ int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq,
 const char* pf_tiled_last_error(void);
 
 /*
+ * Tuning of the large-block path (no reference counterpart; set by the
+ * autotuner in phinfortran_gb300/autotune.py).  panel: width of the panels
+ * of the blocked Gauss-Jordan inverse (4, 8, 16 or 32; narrowed further
+ * when a panel does not fit in shared memory); batch: most points a batch
+ * (1..256).  0 restores the built-in choice.  Process-wide; set it before
+ * sizing the workspace, which depends on it.  pf_tiled_layout reports the
+ * panel width and batch a call of that shape would use.
+ */
+int pf_tiled_set_tuning(int panel, int batch);
+int pf_tiled_layout(int n, int nl, int nr, int npts, int arith, int* panel, int* batch);
+
+/*
  * Batched FP64-grade complex GEMM on the tcgen05 tensor cores.  No
  * counterpart in the reference (it is the block product the large-block
  * transport path is built on, exported for drivers that keep their own

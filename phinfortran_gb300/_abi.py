@@ -78,6 +78,8 @@ SIGNATURES = {
                                             C.c_void_p, C.c_size_t, C.c_void_p]),
     "pf_modes_last_error": (C.c_char_p, []),
     "pf_mixed_stage_timing": (C.c_int, [C.c_int]),
+    "pf_tiled_set_tuning": (C.c_int, [C.c_int, C.c_int]),
+    "pf_tiled_layout": (C.c_int, [C.c_int] * 5 + [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "pf_mixed_stage_times": (C.c_int, [C.POINTER(C.c_float), C.c_int]),
     "pf_transport_tdb_blocks_workspace_size": (C.c_size_t, [C.c_int] * 5),
     "pf_transport_tdb_blocks_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,

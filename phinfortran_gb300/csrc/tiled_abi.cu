@@ -42,6 +42,10 @@ int cuda_err(cudaError_t e, const char* where) {
 
 constexpr int kMaxBatch = 256;
 constexpr size_t kBatchBytes = (size_t)6 << 30;
+// Tuning set by pf_tiled_set_tuning (0: the built-in choice): the panel
+// width of the blocked Gauss-Jordan inverse and the most points a batch.
+int g_tune_panel = 0;
+int g_tune_batch = 0;
 constexpr size_t kSmallInvBytes = 200 * 1024;
 constexpr size_t kPanelBytes = 200 * 1024;
 constexpr int kMats = 16;  // per-point working matrices
@@ -245,7 +249,7 @@ TLayout tlayout(int n, int nl, int nr, int npts, size_t cxb, bool tc = false) {
   l.nr = nr;
   l.m = std::max(n, std::max(nl, nr));
   l.mat = (size_t)l.m * l.m;
-  int nb = 32;
+  int nb = g_tune_panel > 0 ? g_tune_panel : 32;
   while (nb > 4 && ((size_t)l.m * nb + l.m) * cxb > kPanelBytes) nb >>= 1;
   l.nb = nb;
   size_t per_point = (kMats * l.mat + 2 * (size_t)l.m * nb + (size_t)nb * nb + 8) * cxb + (size_t)l.m * 4 + 64;
@@ -253,6 +257,7 @@ TLayout tlayout(int n, int nl, int nr, int npts, size_t cxb, bool tc = false) {
   size_t b = kBatchBytes / per_point;
   if (b < 1) b = 1;
   if (b > (size_t)kMaxBatch) b = kMaxBatch;
+  if (g_tune_batch > 0 && (size_t)g_tune_batch < b) b = g_tune_batch;
   if (npts > 0 && (size_t)npts < b) b = npts;
   l.batch = (int)b;
   return l;
@@ -677,6 +682,26 @@ int drive(int n, int nl, int nr, int L, int nq, const double* const blk[8], int 
 extern "C" {
 
 const char* pf_tiled_last_error(void) { return g_err; }
+
+int pf_tiled_set_tuning(int panel, int batch) {
+  if (panel != 0 && panel != 4 && panel != 8 && panel != 16 && panel != 32)
+    return set_err(PF_ERR_ARG, "pf_tiled_set_tuning: panel must be 0, 4, 8, 16 or 32");
+  if (batch < 0 || batch > kMaxBatch) return set_err(PF_ERR_ARG, "pf_tiled_set_tuning: batch must be in [0, 256]");
+  g_tune_panel = panel;
+  g_tune_batch = batch;
+  return PF_SUCCESS;
+}
+
+int pf_tiled_layout(int n, int nl, int nr, int npts, int arith, int* panel, int* batch) {
+  if (n <= 0 || nl <= 0 || nr <= 0 || npts < 0 || !panel || !batch)
+    return set_err(PF_ERR_ARG, "pf_tiled_layout: bad arguments");
+  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64 && arith != PF_ARITH_TC)
+    return set_err(PF_ERR_ARG, "pf_tiled_layout: unknown arithmetic");
+  const TLayout L2 = tlayout(n, nl, nr, npts, 16, arith == PF_ARITH_TC);
+  *panel = L2.nb;
+  *batch = L2.batch;
+  return PF_SUCCESS;
+}
 
 size_t pf_transport_tdb_tiled_workspace_size(int n, int nl, int nr, int L, int nq, int npts, int arith) {
   if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0) return 0;

@@ -103,3 +103,27 @@ def test_argument_validation_of_tensor_core_and_mixed_entries_without_gpu(built_
     buf = (C.c_float * 3)()
     lib.pf_mixed_stage_timing(0)
     assert lib.pf_mixed_stage_times(buf, 3) == -1
+
+
+def test_tiled_tuning_knobs_without_gpu(built_lib):
+    """The large-block tuning knobs are validated and reported on the host:
+    a panel width outside {0, 4, 8, 16, 32} is refused, a requested panel
+    is narrowed when it does not fit in shared memory, and the batch is
+    capped by the request and by the number of points."""
+    import ctypes as C
+
+    from phinfortran_gb300 import _abi
+    lib = _abi.load()
+    assert lib.pf_tiled_set_tuning(5, 0) == -1
+    p, b = C.c_int(), C.c_int()
+    try:
+        assert lib.pf_tiled_set_tuning(32, 64) == 0
+        assert lib.pf_tiled_layout(96, 96, 96, 1000, 0, C.byref(p), C.byref(b)) == 0
+        assert (p.value, b.value) == (32, 64)
+        assert lib.pf_tiled_layout(768, 768, 768, 10, 0, C.byref(p), C.byref(b)) == 0
+        assert p.value <= 8 and b.value == 10
+        assert lib.pf_tiled_set_tuning(0, 0) == 0
+        assert lib.pf_tiled_layout(96, 96, 96, 1000, 0, C.byref(p), C.byref(b)) == 0
+        assert p.value == 32 and b.value == 256
+    finally:
+        lib.pf_tiled_set_tuning(0, 0)
