@@ -528,9 +528,9 @@ def main():
         torch.backends.cuda.matmul.allow_tf32 = False
         pipe_peak = measure_peak(torch, torch.complex64, 4096)
         pipe = "fp32-simt"
-        pipe_src = ("cuBLAS CGEMM 4096^3 (FP32 SIMT, TF32 off) measured live on this GPU: the 32-wide mixed "
-                    "pipeline runs its matrix work on the FP32 pipe (FP32 and double-float arithmetic); the tensor "
-                    "cores carry the large-block path (large_blocks)")
+        pipe_src = ("cuBLAS CGEMM 4096^3 (FP32 SIMT, TF32 off) measured live on this GPU: the sweeps of the "
+                    "32-wide mixed pipeline run on the FP32 pipe (FP32 and double-float arithmetic); the lead "
+                    "decimations on the tensor cores and the FP64 pipe (see roofline.kernel)")
         kernel = ("mixed pipeline per step (one CUDA-graph replay): leads_tc_kernel (FP64-grade decimation, "
                   "its block products on tcgen05, one CTA per SM) + layer_kernel (warp per point: FP32 LU, back "
                   "substitution, refinement corrections, Caroli; the adaptive second sweep with a CTA per listed "
