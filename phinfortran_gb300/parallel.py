@@ -7,8 +7,12 @@ zero array and an all-reduce SUM over disjoint supports assembles the whole
 table on every rank.
 
 ``shard_points`` balances contiguous chunks by an estimated cost per point
-(n^3 (L + I) for the transport solve: constant within one block set, so by
-default every point costs the same); ``gather_sum`` is the reduction;
+(n^3 (L + I) for the transport solve); ``shard_indices`` is the default of
+the replica runner: without a cost estimate it deals the points out
+strided (point i to rank i mod world), because the decimation count I
+varies smoothly with the energy (more iterations near subband edges and
+band bottoms), so contiguous chunks of an energy grid would give some
+ranks the expensive stretches; ``gather_sum`` is the reduction;
 ``transport_tdb_replicas`` runs `transport_tdb` on this rank's shard and
 gathers T_L (and the status words) on every rank.
 """
@@ -34,14 +38,29 @@ def shard_points(npts, world, rank, cost=None):
     return cuts[rank], cuts[rank + 1]
 
 
-def gather_sum(local, lo, hi, npts, group=None, dtype=None):
-    """Full (npts, ...) array on every rank from each rank's [lo, hi) slice
-    (all-reduce SUM over disjoint supports)."""
+def shard_indices(npts, world, rank, cost=None):
+    """This rank's point indices: strided (rank, rank + world, ...) without a
+    cost estimate, else the contiguous cost-balanced chunk of shard_points."""
+    if world <= 0 or not (0 <= rank < world):
+        raise ValueError("bad world / rank")
+    if cost is None:
+        return np.arange(rank, npts, world)
+    lo, hi = shard_points(npts, world, rank, cost)
+    return np.arange(lo, hi)
+
+
+def gather_sum(local, lo, hi, npts, group=None, dtype=None, idx=None):
+    """Full (npts, ...) array on every rank from each rank's [lo, hi) slice,
+    or its entries at the indices idx (all-reduce SUM over disjoint
+    supports)."""
     import torch
     import torch.distributed as dist
     local = np.asarray(local)
     full = np.zeros((npts,) + local.shape[1:], dtype=dtype or local.dtype)
-    full[lo:hi] = local
+    if idx is None:
+        full[lo:hi] = local
+    else:
+        full[np.asarray(idx)] = local
     t = torch.from_numpy(full)
     backend = dist.get_backend(group) if dist.is_initialized() else None
     if backend == "nccl":
@@ -61,15 +80,15 @@ def transport_tdb_replicas(E, blocks, *, solve=None, group=None, cost=None, **kw
     rank = dist.get_rank(group) if dist.is_initialized() else 0
     E = np.asarray(E, dtype=np.float64)
     npts = E.size
-    lo, hi = shard_points(npts, world, rank, cost)
+    idx = shard_indices(npts, world, rank, cost)
     sub = dict(kw)
     for key in ("qidx", "zero_flag"):
         if sub.get(key) is not None:
-            sub[key] = np.asarray(sub[key])[lo:hi]
-    if hi > lo:
-        r = solve(E[lo:hi], blocks, **sub)
+            sub[key] = np.asarray(sub[key])[idx]
+    if idx.size:
+        r = solve(E[idx], blocks, **sub)
         tl, st = r["transl"], r["status"]
     else:
         tl, st = np.zeros(0), np.zeros(0, np.int32)
-    return dict(transl=gather_sum(tl, lo, hi, npts, group, np.float64),
-                status=gather_sum(st, lo, hi, npts, group, np.int32), shard=(lo, hi))
+    return dict(transl=gather_sum(tl, 0, 0, npts, group, np.float64, idx=idx),
+                status=gather_sum(st, 0, 0, npts, group, np.int32, idx=idx), shard=idx)

@@ -7,7 +7,7 @@ import socket
 import numpy as np
 import pytest
 
-from phinfortran_gb300.parallel import shard_points
+from phinfortran_gb300.parallel import shard_indices, shard_points
 
 
 def test_shard_points_cover_and_balance():
@@ -22,6 +22,21 @@ def test_shard_points_cover_and_balance():
     cost = np.r_[np.full(10, 10.0), np.ones(90)]       # expensive first points
     lo, hi = shard_points(100, 2, 0, cost)
     assert 0 < hi < 60
+
+
+def test_strided_shards_spread_a_cost_ramp():
+    """Without a cost estimate the points are dealt out strided: every point
+    once, and a cost that rises along the energy grid (the decimation count
+    near a band edge) is split evenly, unlike contiguous chunks."""
+    for npts, world in ((0, 2), (13, 2), (1024, 8), (7, 3)):
+        idx = [shard_indices(npts, world, r) for r in range(world)]
+        assert np.array_equal(np.sort(np.concatenate(idx)), np.arange(npts))
+    ramp = np.linspace(10.0, 40.0, 1024)                  # iterations rising along the grid
+    strided = [ramp[shard_indices(1024, 8, r)].sum() for r in range(8)]
+    chunks = [ramp[slice(*shard_points(1024, 8, r))].sum() for r in range(8)]
+    assert max(strided) / min(strided) < 1.02
+    assert max(chunks) / min(chunks) > 2.0
+    assert np.array_equal(shard_indices(100, 2, 0, np.ones(100)), np.arange(50))
 
 
 def fake_solve(E, blocks, qidx=None, zero_flag=None, scale=1.0):
@@ -57,4 +72,4 @@ def test_two_rank_gather(tmp_path):
     for rank in (0, 1):
         np.testing.assert_array_equal(np.load(tmp_path / f"r{rank}.npy"), want)
     s0, s1 = np.load(tmp_path / "s0.npy"), np.load(tmp_path / "s1.npy")
-    assert s0[0] == 0 and s0[1] == s1[0] and s1[1] == 13
+    assert np.array_equal(s0, np.arange(0, 13, 2)) and np.array_equal(s1, np.arange(1, 13, 2))
