@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libphinfortran_gb300.so")
 
-SOURCES = ["negf_abi.cu", "negf_mixed.cu", "dyn_abi.cu", "cond_abi.cu", "grad_abi.cu", "grad_fp64.cu", "grad_df64.cu", "modes_abi.cu", "tiled_abi.cu", "tb_abi.cu", "fullh_abi.cu", "probe_abi.cu", "tc_abi.cu"]
+SOURCES = ["negf_abi.cu", "negf_mixed.cu", "negf_fused.cu", "dyn_abi.cu", "cond_abi.cu", "grad_abi.cu", "grad_fp64.cu", "grad_df64.cu", "modes_abi.cu", "tiled_abi.cu", "tb_abi.cu", "fullh_abi.cu", "probe_abi.cu", "tc_abi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", os.path.join(ROOT, "include")]

@@ -102,7 +102,7 @@ __device__ __forceinline__ fcx f_of(dcx a) { return mk<float>(a.x.hi, a.y.hi); }
 __device__ __forceinline__ dcx d_of(fcx a) { return mk<df64>(df64(a.x, 0.f), df64(a.y, 0.f)); }
 
 // dst(float) = src(df64) or its conjugate transpose
-__device__ void cvt_df_to_f(fcx* dst, int ldd, bool conj_t, const dcx* src, int lds, int m, int n) {
+__device__ inline void cvt_df_to_f(fcx* dst, int ldd, bool conj_t, const dcx* src, int lds, int m, int n) {
   for (int i = threadIdx.x; i < m * n; i += blockDim.x) {
     const int r = i % m, c = i / m;
     const dcx v = conj_t ? cconj(src[c + r * lds]) : src[r + c * lds];
@@ -110,7 +110,7 @@ __device__ void cvt_df_to_f(fcx* dst, int ldd, bool conj_t, const dcx* src, int 
   }
   __syncthreads();
 }
-__device__ void cvt_f_to_df(dcx* dst, int ldd, const fcx* src, int lds, int m, int n) {
+__device__ inline void cvt_f_to_df(dcx* dst, int ldd, const fcx* src, int lds, int m, int n) {
   for (int i = threadIdx.x; i < m * n; i += blockDim.x) {
     const int r = i % m, c = i / m;
     dst[r + (size_t)c * ldd] = d_of(src[r + c * lds]);
@@ -209,7 +209,7 @@ __device__ void copy_cvt(cx<A>* dst, int ldd, bool conj_t, const cx<B>* src, int
 // Helpers of the tensor-core decimation that keep work off the FP64 pipe.
 // W = z - e: the negation as a flip of the sign bit (integer operation),
 // one FP64 addition on the diagonal.
-__device__ void shift_neg_bits(cx<double>* dst, int ldd, cx<double> z, const cx<double>* src, int lds, int n) {
+__device__ inline void shift_neg_bits(cx<double>* dst, int ldd, cx<double> z, const cx<double>* src, int lds, int n) {
   for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
     const int r = i % n, c = i / n;
     const cx<double> v = src[r + c * lds];
@@ -226,7 +226,7 @@ __device__ void shift_neg_bits(cx<double>* dst, int ldd, cx<double> z, const cx<
 // evaluation; equal to a few ulps, so the stopping step can differ from the
 // FP64 path's only when the test value sits within rounding of the
 // threshold).  NaN propagates.
-__device__ double max_mod_sq(const cx<double>* a, int ld, int m, double* red) {
+__device__ inline double max_mod_sq(const cx<double>* a, int ld, int m, double* red) {
   double v = 0.0;
   for (int i = threadIdx.x; i < m * m; i += blockDim.x) {
     const cx<double> e = a[i % m + (i / m) * ld];
@@ -303,7 +303,7 @@ __device__ __forceinline__ int la_pivot(cx<double> v, int lane, int n, bool used
   return st;
 }
 
-__device__ int inverse_la(cx<double>* M, cx<double>* T, int ld, int n, LaWork w) {
+__device__ inline int inverse_la(cx<double>* M, cx<double>* T, int ld, int n, LaWork w) {
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
   int st = PF_OK;
   bool used = false;  // warp 0, lane r: row r has been a pivot
@@ -527,7 +527,7 @@ __device__ int sancho_step(const Ctx<R>& c, int m, cx<R> z) {
 
 // In-place FP64 -> df64 of an m x m slot (both 16 bytes per complex element;
 // every element is read and written by the same thread).
-__device__ void slot_to_df64(dcx* a, int ld, int m) {
+__device__ inline void slot_to_df64(dcx* a, int ld, int m) {
   for (int i = threadIdx.x; i < m * m; i += blockDim.x) {
     const int r = i % m, c = i / m;
     const cx<double> v = reinterpret_cast<const cx<double>*>(a)[r + c * ld];
@@ -740,7 +740,7 @@ __device__ __forceinline__ dcx ell_row_dot(const Ell& e, size_t blk, int r, cons
 
 // Interior residual layer j (1..L) with sparse blocks, one pass:
 // R = - z X_j + Hd_j X_j + V_{j-1}^H X_{j-1} + V_j X_{j+1}
-__device__ void residual_sparse(const MSys& s, int q, int j, dcx zD, const dcx* Xm, const dcx* X0, const dcx* Xp,
+__device__ inline void residual_sparse(const MSys& s, int q, int j, dcx zD, const dcx* Xm, const dcx* X0, const dcx* Xp,
                                 dcx* R, int ld) {
   const int n = s.n, nr = s.nr, L = s.L;
   for (int i = threadIdx.x; i < n * nr; i += blockDim.x) {

@@ -17,25 +17,7 @@ using pf::cx;
 // message of the last error of the tdb entries (defined in negf_abi.cu)
 extern thread_local char pf_negf_err[512];
 
-namespace {
-
-int set_err(int code, const char* msg) {
-  snprintf(pf_negf_err, sizeof(pf_negf_err), "%s", msg);
-  return code;
-}
-int cuda_err(cudaError_t e, const char* where) {
-  snprintf(pf_negf_err, sizeof(pf_negf_err), "%s: %s", where, cudaGetErrorString(e));
-  return PF_ERR_CUDA;
-}
-
-#define PF_CUDA(call)                               \
-  do {                                              \
-    cudaError_t e_ = (call);                        \
-    if (e_ != cudaSuccess) return cuda_err(e_, #call); \
-  } while (0)
-
-constexpr int kThreads = 256;
-constexpr int kMixedThreads = 512;  // fused mixed kernel (blocks above 32): one CTA per SM, 16 warps per point
+namespace pfn {
 
 // Layout of the per-CTA scratch: NG matrices of ld*m elements.
 struct Layout {
@@ -59,6 +41,30 @@ Layout make_layout(int n, int nl, int nr) {
   l.per_cta_bytes = (size_t)pf::NG * l.mat * cxb;
   return l;
 }
+
+}  // namespace pfn
+
+namespace {
+
+int set_err(int code, const char* msg) {
+  snprintf(pf_negf_err, sizeof(pf_negf_err), "%s", msg);
+  return code;
+}
+int cuda_err(cudaError_t e, const char* where) {
+  snprintf(pf_negf_err, sizeof(pf_negf_err), "%s: %s", where, cudaGetErrorString(e));
+  return PF_ERR_CUDA;
+}
+
+#define PF_CUDA(call)                               \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return cuda_err(e_, #call); \
+  } while (0)
+
+constexpr int kThreads = 256;
+
+using pfn::Layout;
+using pfn::make_layout;
 
 
 

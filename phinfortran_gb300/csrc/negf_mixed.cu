@@ -3,15 +3,12 @@
 // cores for blocks up to 32), FP32 block LU of the device, double-float
 // refinement and Caroli trace.  The host-pointer entry
 // pf_transport_tdb_mixed is in negf_abi.cu.
-#include "negf_common.cuh"
-#include "warp_engine.cuh"
+#include "negf_fused.cuh"
 
 namespace {
 // ===========================================================================
 // Mixed-precision path
 // ===========================================================================
-using pf::dcx;
-using pf::fcx;
 
 // FP64 -> df64 and FP32 copies of a block array (grid-stride)
 __global__ void convert_blocks_kernel(const cx<double>* src, dcx* d, fcx* f, size_t count) {
@@ -55,118 +52,9 @@ __global__ void build_ell_kernel(const dcx* M, int rows, int cols, int count, in
   }
 }
 
-struct MixedLayout {
-  Layout base;     // smem slots are df64-sized (16 B per complex)
-  size_t smem;
-  size_t smem_leads;  // the leads kernel needs only the NSM decimation slots
-  size_t per_cta;  // bytes of per-CTA scratch
-  size_t blocks_d, blocks_f;  // bytes of converted block copies (per call)
-  size_t cnt[8];   // complex elements per block family (all q)
-  size_t ell_rows[7];  // ELL rows: Hd, Hdv, Hdv^H, Hld, Hld^H, Hrd, Hrd^H
-  size_t ell_bytes;
-};
-
-MixedLayout make_mixed_layout(int n, int nl, int nr, int L, int nq) {
-  MixedLayout m;
-  m.base = make_layout<double>(n, nl, nr);
-  const size_t mat = m.base.mat;
-  const size_t tail = 32 * sizeof(double) + 2 * (size_t)m.base.m * 16 + (size_t)m.base.m * sizeof(int) +
-                      64 * sizeof(int);
-  m.smem = pf::NSM_M * mat * 16 + tail;
-  m.smem_leads = pf::NSM * mat * 16 + tail;
-  const size_t nslab = (size_t)(L + 2);
-  m.per_cta = ((size_t)pf::NGM * mat * 16 + nslab * mat * (8 + 8 + 16) + mat * 8 + 255) & ~(size_t)255;
-  const size_t c[8] = {(size_t)nq * nl * nl, (size_t)nq * nl * nl, (size_t)nq * nr * nr, (size_t)nq * nr * nr,
-                       (size_t)nq * L * n * n, (size_t)nq * (L > 1 ? L - 1 : 0) * n * n, (size_t)nq * nl * n,
-                       (size_t)nq * nr * n};
-  size_t tot = 0;
-  for (int i = 0; i < 8; ++i) {
-    m.cnt[i] = c[i];
-    tot += (c[i] * 16 + 255) & ~(size_t)255;
-  }
-  m.blocks_d = tot;
-  size_t totf = 0;
-  for (int i = 2; i < 8; ++i) totf += (c[i] * 8 + 255) & ~(size_t)255;  // HR, HRv(unused), Hd, Hdv, Hld, Hrd
-  m.blocks_f = totf;
-  const size_t er[7] = {(size_t)nq * L * n, (size_t)nq * (L > 1 ? L - 1 : 0) * n,
-                        (size_t)nq * (L > 1 ? L - 1 : 0) * n, (size_t)nq * nl, (size_t)nq * n, (size_t)nq * nr,
-                        (size_t)nq * n};
-  size_t eb = 256;  // overflow flag
-  for (int i = 0; i < 7; ++i) {
-    m.ell_rows[i] = er[i];
-    eb += ((er[i] * pf::PF_ELL_K * 4 + 255) & ~(size_t)255) + ((er[i] * pf::PF_ELL_K * 16 + 255) & ~(size_t)255);
-  }
-  m.ell_bytes = eb + (((size_t)nq * sizeof(int) + 255) & ~(size_t)255);  // + lead mirror flags
-  return m;
-}
-
-template <int S>
-__global__ void __launch_bounds__(kMixedThreads) mixed_kernel(pf::MSys sys, pf::Points pts, pf::Params P, int nref,
-                                                         pf::Outputs out, MixedLayout lay, char* scratch,
-                                                         int* queue) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  pf::MCtx c;
-  const size_t mat = lay.base.mat;
-  dcx* s = reinterpret_cast<dcx*>(smem_raw);
-  for (int i = 0; i < pf::NSM_M; ++i) c.sm[i] = s + i * mat;
-  unsigned char* tail = reinterpret_cast<unsigned char*>(s + pf::NSM_M * mat);
-  c.red = reinterpret_cast<double*>(tail);
-  c.iwd.rowk = reinterpret_cast<dcx*>(tail + 32 * sizeof(double));
-  c.iwd.colk = c.iwd.rowk + lay.base.m;
-  int* ip = reinterpret_cast<int*>(c.iwd.colk + lay.base.m);
-  c.iwd.perm = ip;
-  c.iwd.flag = ip + lay.base.m;
-  c.iwf.rowk = reinterpret_cast<fcx*>(c.iwd.rowk);
-  c.iwf.colk = reinterpret_cast<fcx*>(c.iwd.colk);
-  c.iwf.perm = c.iwd.perm;
-  c.iwf.flag = c.iwd.flag;
-  char* base = scratch + (size_t)blockIdx.x * lay.per_cta;
-  dcx* g = reinterpret_cast<dcx*>(base);
-  for (int i = 0; i < pf::NGM; ++i) c.gs[i] = g + i * mat;
-  const size_t nslab = (size_t)(sys.L + 2);
-  c.xv = g + pf::NGM * mat;
-  c.lu = reinterpret_cast<fcx*>(c.xv + nslab * mat);
-  c.yv = c.lu + nslab * mat;
-  c.fsr = c.yv + nslab * mat;
-  c.ld = lay.base.ld;
-  c.mat = mat;
-  __shared__ int s_p;
-  for (;;) {
-    if (threadIdx.x == 0) s_p = atomicAdd(queue, 1);
-    __syncthreads();
-    const int p = s_p;
-    __syncthreads();
-    if (p >= pts.npts) break;
-    const int q = pts.qidx ? pts.qidx[p] : 0;
-    const double E = pts.E[p];
-    int itl = 0, itr = 0;
-    int st = pf::mixed_leads<S>(c, sys, q, E, P, &itl, &itr);
-    const double eps = E * P.eta + P.eta0;
-    const fcx zf = pf::mk<float>((float)E, (float)(P.dev_factor * eps));
-    st |= pf::mixed_factor_solve<S>(c, sys, q, zf);
-    const dcx zL = pf::mk<pf::df64>(pf::df64(E), pf::df64(eps));
-    const dcx zD = pf::mk<pf::df64>(pf::df64(E), pf::df64(P.dev_factor * eps));
-    // the first sweep always; later ones while the last correction of X_0
-    // was above PF_REFINE_TOL
-    for (int k = 0; k < nref; ++k)
-      if (!pf::mixed_refine<S>(c, sys, q, zL, zD)) break;
-    const double tl = pf::mixed_caroli<S>(c, sys);
-    if (threadIdx.x == 0) {
-      const bool zero = pts.zero_flag && pts.zero_flag[p];
-      double a = tl;
-      if (zero || a < 1.0e-60) a = 0.0;
-      if (!(a == a)) st |= pf::PF_NAN;
-      out.transl[p] = a;
-      out.status[p] = st;
-      if (out.iters) {
-        out.iters[2 * p] = itl;
-        out.iters[2 * p + 1] = itr;
-      }
-    }
-    __syncthreads();
-  }
-}
-
+using pfn::MixedLayout;
+using pfn::make_mixed_layout;
+using pfn::kMixedThreads;
 
 // ---------------------------------------------------------------------------
 // Mixed path, cross-sections <= 32: leads kernel (CTA per point) + layer
@@ -756,10 +644,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, kLayerCtasPerSm)
 
 template <int S>
 int mixed_grid(const MixedLayout& lay, int npts) {
-  auto k = mixed_kernel<S>;
-  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.smem) != cudaSuccess) return -1;
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kMixedThreads, lay.smem) != cudaSuccess) return -1;
+  const int per_sm = pfn::fused_per_sm(S, lay.smem);
   if (per_sm < 1) return -1;
   DevInfo d = device_info();
   int g = d.sms * per_sm;
@@ -830,7 +715,7 @@ bool make_plan(int n, int nl, int nr, int L, int nq, int npts, MixedPlan& P) {
       return false;
     P.grid_r = d.sms * per_sm_r;
   } else {
-    P.grid_a = (S == 1) ? mixed_grid<1>(lay, np) : mixed_grid<2>(lay, np);
+    P.grid_a = mixed_grid<2>(lay, np);  // 32 < m <= 64
     P.per_cta_a = lay.per_cta;
     P.grid_b = 0;
     P.grid_r = 0;
@@ -1078,10 +963,8 @@ int mixed_launch(const MixedPlan& plan, int n, int nl, int nr, int L, int nq, co
     layer_kernel<<<plan.grid_b, kWarpsPerCta * 32, plan.smem_b, st>>>(sys, pts, P, 2, out, lo, sl, lstat, queue_b,
                                                                        nullptr, nullptr);
     g_timer.mark(3, st);
-  } else if (S == 1) {
-    mixed_kernel<1><<<plan.grid_a, kMixedThreads, lay.smem, st>>>(sys, pts, P, refine_iters, out, lay, scratch, queue);
   } else {
-    mixed_kernel<2><<<plan.grid_a, kMixedThreads, lay.smem, st>>>(sys, pts, P, refine_iters, out, lay, scratch, queue);
+    PF_CUDA(pfn::fused_launch(S, plan.grid_a, lay.smem, st, sys, pts, P, refine_iters, out, lay, scratch, queue));
   }
   PF_CUDA(cudaGetLastError());
   return PF_SUCCESS;

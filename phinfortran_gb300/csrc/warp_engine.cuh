@@ -182,7 +182,7 @@ __device__ __forceinline__ void stage_rows(fcx* S, const GView& g, int lane) {
 // (ld 32).  Lane r owns row r, so every shared access is either a row-r
 // element (consecutive lanes, conflict free) or a broadcast of the pivot
 // row.  Returns status bits (uniform).
-__device__ int winverse(fcx* S, fcx* D, fcx* gout, int lane) {
+__device__ inline int winverse(fcx* S, fcx* D, fcx* gout, int lane) {
   unsigned used = 0u;
   int status = PF_OK;
   int perm_mine = 0;  // P[lane]: pivot row of step `lane`
