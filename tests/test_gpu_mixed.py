@@ -93,6 +93,31 @@ def test_mixed_edge_shapes(cuda_ready):
         assert np.abs(r["transl"] - o["transl"]).max() < 1e-9, L
 
 
+def test_mixed_tensor_core_leads_of_two_widths(cuda_ready):
+    """The tensor-core lead decimations with a 28-wide left lead and a
+    32-wide right lead in the same call (the operand tiles are re-zeroed
+    when the block size changes from one product to the next), random
+    Hermitian blocks, against the oracle."""
+    rng = np.random.default_rng(11)
+    n, nl, nr, L = 30, 28, 32, 4
+
+    def herm(m):
+        a = rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m))
+        return (a + a.conj().T) * 0.5
+
+    blocks = dict(HL=herm(nl), HLv=rng.normal(size=(nl, nl)) * 0.3, HR=herm(nr),
+                  HRv=rng.normal(size=(nr, nr)) * 0.3, Hd=np.array([herm(n) for _ in range(L)]),
+                  Hdv=rng.normal(size=(L - 1, n, n)) * 0.3, Hld=rng.normal(size=(nl, n)) * 0.3,
+                  Hrd=rng.normal(size=(nr, n)) * 0.3)
+    E = np.linspace(-2.5, 2.5, 11)
+    r = transport_tdb(E, blocks, eta=0.0, eta0=1e-4, convergence=1e-13, dev_factor=1.0,
+                      precision="mixed", refine_iters=2)
+    o = N.transport(E, blocks, 0.0, 1e-4, 1e-13, 1.0)
+    assert (r["status"] == 0).all()
+    assert np.abs(r["transl"] - o["transl"]).max() < 1e-8 * max(1.0, np.abs(o["transl"]).max())
+    assert np.abs(r["iters"][:, 0] - o["iters_left"]).max() <= 1
+
+
 @pytest.mark.parametrize("precision,ne", [("fp64", 96), ("mixed", 96), ("mixed", 300)])
 def test_graph_replay_matches_direct_run(cuda_ready, precision, ne):
     """The batched pass captured into a CUDA graph and replayed gives the
