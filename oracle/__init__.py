@@ -2,8 +2,8 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the shipped package imports this
 directory; only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline
-leg of ``bench.py`` use it, always as the checker and never as the code under
-measurement.
+leg of ``bench.py`` use it, always as the reference results are compared
+with and never as the code under measurement.
 
 The modules restate the reference Fortran (KitchenSong/phinfortran) in numpy,
 batched over (omega, q) points but otherwise step for step:

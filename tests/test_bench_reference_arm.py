@@ -1,5 +1,6 @@
-"""bench.py --impl reference (the CPU arm the driver runs beside ours) prints
-one JSON line with the contract's keys (CPU, a short sample)."""
+"""bench.py --impl reference (the CPU reference arm timed beside the GPU
+path) prints one JSON line with the benchmark's keys (CPU, a short
+sample)."""
 import json
 import os
 import subprocess
