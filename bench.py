@@ -12,10 +12,13 @@ T(E) per (E, q) point ("solve").
     python bench.py --impl reference ...   (CPU oracle on the host cores)
 
 Rank 0 prints one JSON line.  `value` = solves/s of the headline path
-(default: mixed precision -- double-float leads, FP32 factorisation,
-double-float refinement: one sweep for every point and a second for the
-points whose first correction was above 3e-5) with inputs resident in HBM (CUDA events
-around each step on the launching stream, L2 flushed before every step);
+(default: mixed precision -- FP64-grade lead decimations with their block
+products on the tensor cores, FP32 factorisation, double-float refinement:
+one sweep for every point and a second for the points whose first
+correction was above 3e-5; one CUDA-graph replay a step) with inputs
+resident in HBM (CUDA events around each step on the launching stream, L2
+flushed before every step); `roofline` = the dominant kernel (the lead
+decimations, timed by the library's stage events);
 `e2e` = the same through the host-pointer C entry with host buffers, copies
 inside the timed region; `compare` = the plain FP64 path on the same batch
 (speed-up and the accuracy of the headline T(E) against it).
@@ -583,7 +586,7 @@ def main():
     if args.path == "fp64":
         launches_per_step = 2                         # lead-mirror check + transport_kernel
     else:
-        # 8 block conversions + 7 ELL builds + lead-mirror check + leads_kernel + layer_kernel (factor)
+        # 8 block conversions + 7 ELL builds + lead-mirror check + leads_tc_kernel + layer_kernel (factor)
         # + the first refinement sweep (residual_kernel + layer_kernel) + each later, adaptive sweep
         # (refine_select_kernel + residual_kernel + layer_kernel) + point-energy kernel + layer_kernel (Caroli)
         sweeps = (2 + 3 * (args.refine - 1) + 1) if args.refine else 0
