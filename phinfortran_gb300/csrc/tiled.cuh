@@ -254,7 +254,13 @@ __global__ void __launch_bounds__(256) gje_panel(cx<T>* A, int lda, long long sA
           const cx<T> t = cmul(f, ip);
           S[r + (size_t)j * n] = mk<T>(-t.x, -t.y);
         } else {
-          S[r + (size_t)j * n] = csub(S[r + (size_t)j * n], cmul(f, prow[j]));
+          // v - f prow_j as two fused multiply-adds a component (four FP64
+          // operations an element instead of six)
+          const cx<T> pj = prow[j];
+          cx<T> v = S[r + (size_t)j * n];
+          v.x = fma(-f.x, pj.x, fma(f.y, pj.y, v.x));
+          v.y = fma(-f.x, pj.y, fma(-f.y, pj.x, v.y));
+          S[r + (size_t)j * n] = v;
         }
       }
     }
