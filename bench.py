@@ -271,7 +271,35 @@ def large_block_sample(torch, sizes=((2, 8, 32), (3, 8, 20), (4, 2, 4))):
                                        tuned_s=best["seconds"], default_s=best["default_seconds"],
                                        candidates=[(c["panel"], c["batch"], c["seconds"]) for c in best["candidates"]],
                                        note="panel 0 / batch 0 = the built-in choice")
+    out.append(circular_sample(torch))
     return out
+
+
+def circular_sample(torch, nc=3, ne=64):
+    """Block-circulant leads (circular_flag = 1): the diamond slab at the
+    transverse Gamma point has nc x nc block-circulant lead matrices; the
+    lead surface Green's functions through circular_g (K = nc^2 small
+    decimations of 24 x 24 per point) against the decimation of the full
+    n x n lead matrices, tensor-core block products, L = 60, ne points."""
+    from phinfortran_gb300 import systems as S, transport_tdb
+    b, E, p, aux = S.diamond_phonon(nc=nc, L=60, nk_side=1, ne=ne)
+    bq = {k: v[0] for k, v in b.items()}
+    res = {}
+    for mode in ("full", "circular"):
+        kw = dict(circular=(nc, nc, [2.0 * np.pi] * 4)) if mode == "circular" else {}
+        transport_tdb(E[:2], bq, want_transr=False, precision="tc", **kw, **p)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = transport_tdb(E, bq, want_transr=False, check=False, precision="tc", **kw, **p)
+        torch.cuda.synchronize()
+        res[mode] = (time.perf_counter() - t0, r)
+    Tf, Tc = res["full"][1]["transl"], res["circular"][1]["transl"]
+    return dict(n=aux["n"], L=60, points=int(E.size), circular=dict(n_bloch_y=nc, n_bloch_x=nc, small_block=24),
+                full_solves_per_s=E.size / res["full"][0], circular_solves_per_s=E.size / res["circular"][0],
+                circular_speedup=res["full"][0] / res["circular"][0],
+                max_rel_dev=float((np.abs(Tc - Tf) / np.maximum(np.abs(Tf), 1e-3)).max()),
+                status_nonzero={k: int((res[k][1]["status"] != 0).sum()) for k in res},
+                note="host-pointer call, tensor-core products; deviation = max |T_circ - T_full| / max(|T_full|, 1e-3)")
 
 
 def gradient_ratio(torch, flush, stream, steps):

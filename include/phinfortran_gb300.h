@@ -524,6 +524,43 @@ int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq,
                                double* transl, int* status, int* iters,
                                void* work, size_t work_bytes, void* stream);
 
+/* pf_transport_tdb_tiled_dev with circular_flag = 1: the lead surface
+ * Green's functions through circular_g (negf/circular.f90:42-105, called
+ * from surface_green_tdb, negf/surface.f90:498-501 and :558-562) instead of
+ * the decimation of the full lead matrices.  The leads are block circulant
+ * over n_bloch_y x n_bloch_x Bloch cells (nl == nr, a multiple of
+ * n_bloch_y * n_bloch_x): the first block rows of H00 and of the coupling are
+ * Fourier-transformed along y (n_bloch_y outer blocks) and then x
+ * (n_bloch_x inner blocks) (util.f90:732-756), the K = n_bloch_y * n_bloch_x
+ * small blocks of nl / K are decimated on their own with beta = alpha^H
+ * (util.f90:761-799), and the result is transformed back with the unitary
+ * matrices of set_pmatrix (circular.f90:9-38).  gr (host, 4 doubles): the
+ * G.R products of the forward transforms, {left y, left x, right y, right x}
+ * = {reci_uc_l(2,:).latvec_uc_l(2,:), reci_uc_l(1,:).latvec_uc_l(1,:), the
+ * same of the right lead}; the back transform takes the left lead's two, as
+ * the reference builds P1, P2 once from the left lead
+ * (negf/phinfortran.f90:622-628).  iters reports, per lead, the most
+ * decimation steps of the K small blocks.  Only the first block rows of the
+ * lead matrices are read, as in the reference, so leads that are not block
+ * circulant give the reference's (wrong) result, not an error.  work:
+ * pf_transport_tdb_tiled_circ_workspace_size bytes (0: invalid arguments). */
+size_t pf_transport_tdb_tiled_circ_workspace_size(int n, int nl, int nr, int L, int nq,
+                                                  int npts, int arith, int n_bloch_y,
+                                                  int n_bloch_x);
+
+int pf_transport_tdb_tiled_circ_dev(int n, int nl, int nr, int L, int nq,
+                                    const double* HL, const double* HLv,
+                                    const double* HR, const double* HRv,
+                                    const double* Hd, const double* Hdv,
+                                    const double* Hld, const double* Hrd,
+                                    int npts, const double* E, const int* qidx,
+                                    const int* zero_flag,
+                                    double eta, double eta0, double dev_factor,
+                                    double convergence, int max_iter, int arith,
+                                    int n_bloch_y, int n_bloch_x, const double* gr,
+                                    double* transl, int* status, int* iters,
+                                    void* work, size_t work_bytes, void* stream);
+
 /* Message for the last error of the large-block entry points. */
 const char* pf_tiled_last_error(void);
 

@@ -83,3 +83,43 @@ def circular_g(Es0, e1, alpha, beta, convergence, n, nb, nc, G1, R1, G2, R2, P1=
             green2[t, t] = decimation(Ey[t, t], ey[t, t], ay[t, t], convergence)
         green1[s, s] = P2[0] @ green2 @ P2[1]
     return P1[0] @ green1 @ P1[1]
+
+
+def transport_circular(E, blocks, eta, eta0, convergence, dev_factor, n_bloch_y, n_bloch_x, gr,
+                       zero_first=None):
+    """T_L of one q with circular_flag = 1: surface_green_tdb's two decimations
+    on the transmission path (left advanced, negf/surface.f90:479-507; right
+    retarded, :540-568) through circular_g, then the wrapper conjugations
+    (negf/lesser.f90:141-144) and the sweep and Caroli trace of
+    get_G_full_tdb (oracle.negf.get_G_full_tdb).  ``gr``: the G.R products
+    {left y, left x, right y, right x}; P1, P2 from the left lead's
+    (negf/phinfortran.f90:622-628)."""
+    from oracle import negf as N
+    E = np.asarray(E, dtype=np.float64)
+    HL, HLv, HR, HRv = (np.asarray(blocks[k], dtype=np.complex128) for k in ("HL", "HLv", "HR", "HRv"))
+    n = HL.shape[0]
+    ny, nx = int(n_bloch_y), int(n_bloch_x)
+    ey, ex = np.array([1.0, 0.0, 0.0]), np.array([0.0, 1.0, 0.0])
+    # G and R enter only through G.R: carry each product on unit vectors
+    GRl = (gr[0] * ey, ey, gr[1] * ex, ex)
+    GRr = (gr[2] * ey, ey, gr[3] * ex, ex)
+    P1 = set_pmatrix(n, ny, GRl[0], GRl[1])
+    P2 = set_pmatrix(n // ny, nx, GRl[2], GRl[3])
+    eps = N.lead_eps(E, eta, eta0)
+    B = E.size
+    gl_adv = np.zeros((B, n, n), np.complex128)
+    gr_ret = np.zeros((B, n, n), np.complex128)
+    for b in range(B):
+        zl, zr = E[b] - 1j * eps[b], E[b] + 1j * eps[b]
+        a = N.H(HLv)
+        gl_adv[b] = circular_g(zl * np.eye(n), HL, a, N.H(a), convergence, n, ny, nx, *GRl, P1=P1, P2=P2)
+        a = N.H(HRv)
+        gr_ret[b] = circular_g(zr * np.eye(n), HR, a, N.H(a), convergence, n, ny, nx, *GRr, P1=P1, P2=P2)
+    sl_adv = N.H(HLv) @ gl_adv @ HLv
+    gml_adv = 1j * (sl_adv - N.H(sl_adv))
+    sr_ret = N.H(HRv) @ gr_ret @ HRv
+    gmr_ret = 1j * (sr_ret - N.H(sr_ret))
+    r = N.get_G_full_tdb(E, N.H(gl_adv), gr_ret, -gml_adv, gmr_ret, N.H(sl_adv), sr_ret,
+                         blocks["Hd"], blocks["Hdv"], blocks["Hld"], blocks["Hrd"], HL, HR,
+                         eta, eta0, dev_factor, zero_first=zero_first)
+    return r["transl"]

@@ -12,6 +12,7 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <cmath>
 #include <type_traits>
 #include <vector>
 
@@ -233,8 +234,136 @@ __global__ void k_mirror(const double* HL, const double* HLv, const double* HR, 
 }
 
 // ---------------------------------------------------------------------------
+// block-circulant leads (circular_flag = 1, negf/circular.f90:42-105)
+//
+// A lead of ny x nx Bloch cells has block-circulant matrices: ny outer
+// blocks of na = m / ny rows, each of them nx inner blocks of s = na / nx.
+// The two-level Fourier transform of their first block rows
+// (util.f90:732-756, applied along y then along x) makes them block
+// diagonal; each of the K = ny nx small s x s blocks is decimated on its own
+// (util.f90:761-799) and the result transformed back with the unitary
+// P1 = F_y (x) 1, P2 = F_x (x) 1 of set_pmatrix (circular.f90:9-38).
+// ---------------------------------------------------------------------------
+// dst_b = op(src_{b mod period}) (src stride ss; ss = 0: one shared source)
+template <typename T>
+__global__ void k_copy_per(cx<T>* dst, long long sd, const cx<T>* src, long long ss, int period, int lds, int rows,
+                           int cols, int ldd, int conj_t) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows * cols) return;
+  const int r = i % rows, c = i / rows;
+  const cx<T>* sp = src + (size_t)(b % period) * ss;
+  const cx<T> v = conj_t ? pf::cconj(sp[c + (size_t)r * lds]) : sp[r + (size_t)c * lds];
+  dst[(size_t)b * sd + r + (size_t)c * ldd] = v;
+}
+// Small block kb = i nx + j (s x s, ld s) of the lead's transforms:
+//   hs[kb](r, c) = sum_l w_x^{j l} sum_p w_y^{i p} h00(r, p na + l s + c)
+// (w_y = exp(i gry / ny), w_x = exp(i grx / nx)); the same of alpha = v^H,
+// stored conjugate-transposed (vs[kb] = alpha_s[kb]^H), the form decimate()
+// takes its coupling in (alpha0 = v^H, beta0 = v; util.f90 decimation sets
+// beta = alpha^H).  Grid (ceil(s*s/256), K).
+template <typename T>
+__global__ void k_circ_fwd(const cx<T>* h00, const cx<T>* v, int m, int ny, int nx, double gry, double grx,
+                           cx<T>* hs, cx<T>* vs) {
+  const int s = m / (ny * nx), na = m / ny;
+  const int kb = blockIdx.y, i = kb / nx, j = kb % nx;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= s * s) return;
+  const int r = e % s, c = e / s;
+  double hr = 0.0, hi = 0.0, ar = 0.0, ai = 0.0;  // alpha_s(c, r) for vs(r, c) = conj(alpha_s(c, r))
+  for (int l = 0; l < nx; ++l) {
+    double h1r = 0.0, h1i = 0.0, a1r = 0.0, a1i = 0.0;
+    for (int p = 0; p < ny; ++p) {
+      double sn, cs;
+      sincos(gry * (double)(i * p) / (double)ny, &sn, &cs);
+      const size_t col_h = (size_t)p * na + (size_t)l * s + c;
+      const cx<T> h = h00[r + col_h * m];
+      h1r += pf::to_d(h.x) * cs - pf::to_d(h.y) * sn;
+      h1i += pf::to_d(h.x) * sn + pf::to_d(h.y) * cs;
+      // alpha(c, col) = conj(v(col, c)), col = p na + l s + r
+      const size_t col_a = (size_t)p * na + (size_t)l * s + r;
+      const cx<T> a = v[col_a + (size_t)c * m];
+      const double xr = pf::to_d(a.x), xi = -pf::to_d(a.y);
+      a1r += xr * cs - xi * sn;
+      a1i += xr * sn + xi * cs;
+    }
+    double sn, cs;
+    sincos(grx * (double)(j * l) / (double)nx, &sn, &cs);
+    hr += h1r * cs - h1i * sn;
+    hi += h1r * sn + h1i * cs;
+    ar += a1r * cs - a1i * sn;
+    ai += a1r * sn + a1i * cs;
+  }
+  hs[(size_t)kb * s * s + r + (size_t)c * s] = pf::mk<T>(T(hr), T(hi));
+  vs[(size_t)kb * s * s + r + (size_t)c * s] = pf::mk<T>(T(ar), T(-ai));
+}
+// g_b = P1 diag_i(P2 diag_j(gs[b K + i nx + j]) P2^H) P1^H:
+//   g((a nx + u) s + r, (a' nx + u') s + c)
+//     = 1/K sum_i w_y^{i (a - a')} sum_j w_x^{j (u - u')} gs[b K + i nx + j](r, c)
+// Grid (ceil(m*m/256), batch).
+template <typename T>
+__global__ void k_circ_back(cx<T>* out, long long so, int ld, const cx<T>* gs, int m, int ny, int nx, double gry,
+                            double grx) {
+  const int b = blockIdx.y;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m * m) return;
+  const int K = ny * nx, s = m / K;
+  const int R = e % m, Cc = e / m;
+  const int a = R / (nx * s), u = (R / s) % nx, r = R % s;
+  const int a2 = Cc / (nx * s), u2 = (Cc / s) % nx, c = Cc % s;
+  const cx<T>* g = gs + (size_t)b * K * s * s + r + (size_t)c * s;
+  double xr = 0.0, xi = 0.0;
+  for (int i = 0; i < ny; ++i) {
+    double yr = 0.0, yi = 0.0;
+    for (int j = 0; j < nx; ++j) {
+      const cx<T> v = g[(size_t)(i * nx + j) * s * s];
+      double sn, cs;
+      sincos(grx * (double)(j * (u - u2)) / (double)nx, &sn, &cs);
+      yr += pf::to_d(v.x) * cs - pf::to_d(v.y) * sn;
+      yi += pf::to_d(v.x) * sn + pf::to_d(v.y) * cs;
+    }
+    double sn, cs;
+    sincos(gry * (double)(i * (a - a2)) / (double)ny, &sn, &cs);
+    xr += yr * cs - yi * sn;
+    xi += yr * sn + yi * cs;
+  }
+  out[(size_t)b * so + R + (size_t)Cc * ld] = pf::mk<T>(T(xr / K), T(xi / K));
+}
+// zs[b K + k] = z[b]; st_s = 0
+template <typename T>
+__global__ void k_circ_points(const cx<T>* z, int B, int K, cx<T>* zs, int* st_s) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= B * K) return;
+  zs[i] = z[i / K];
+  st_s[i] = 0;
+}
+// per point: iterations = the most of its K small decimations, status = their OR
+__global__ void k_circ_fold(const int* it_s, const int* st_s, int B, int K, int* it, int* st) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  int mx = 0, f = 0;
+  for (int k = 0; k < K; ++k) {
+    mx = max(mx, it_s[b * K + k]);
+    f |= st_s[b * K + k];
+  }
+  it[b] = mx;
+  st[b] |= f;
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// Block-circulant leads: ny x nx Bloch cells (n_bloch_y, n_bloch_x) and the
+// G.R products of the y and x lattice vectors of each lead (forward
+// transforms); the back transform uses the left lead's, as the reference
+// builds P1, P2 once from the left lead (negf/phinfortran.f90:622-628).
+struct Circ {
+  int ny = 1, nx = 1;
+  double gr_l[2] = {0.0, 0.0};
+  double gr_r[2] = {0.0, 0.0};
+  int K() const { return ny * nx; }
+};
+
 struct TLayout {
   int n, nl, nr, m, nb, batch;
   size_t mat;  // elements per working matrix (m * m, ld m)
@@ -261,6 +390,21 @@ TLayout tlayout(int n, int nl, int nr, int npts, size_t cxb, bool tc = false) {
   if (npts > 0 && (size_t)npts < b) b = npts;
   l.batch = (int)b;
   return l;
+}
+
+// tlayout with the batch bounded so that the small-block batch of
+// block-circulant leads (batch K) stays within one grid dimension
+TLayout tiled_layout(int n, int nl, int nr, int npts, size_t cxb, bool tc, int K) {
+  TLayout l = tlayout(n, nl, nr, npts, cxb, tc);
+  if (K > 1) l.batch = std::max(1, std::min(l.batch, 65535 / K));
+  return l;
+}
+// layout of the small-block engine: blocks of nl / K, batch K times the main
+TLayout small_layout(const TLayout& L, int K, size_t cxb) {
+  const int sb = L.nl / K;
+  TLayout S = tlayout(sb, sb, sb, 0, cxb, false);
+  S.batch = L.batch * K;
+  return S;
 }
 
 template <typename T>
@@ -322,6 +466,10 @@ struct Engine {
   void* tcw = nullptr;
   size_t tcw_bytes = 0;
   int* tcerr = nullptr;
+  // block-circulant leads: the option and the engine of the small blocks
+  // (batch B K, FP64 or double-float SIMT products)
+  const Circ* circ = nullptr;
+  Engine<T>* small = nullptr;
 
   dim3 eg(int elems) const { return dim3((elems + 255) / 256, B); }
 
@@ -426,8 +574,11 @@ struct Engine {
 
   // Lopez-Sancho decimation of one lead for the batch (surface.f90:479-497)
   // with alpha0 = v^H, beta0 = v; g = inv(z - es) into out.
+  // h00 and v: one shared block (ss = 0) or per point b the block b mod
+  // period at stride ss, leading dimension lds.
   int decimate(int m, const cx<T>* h00, const cx<T>* v, const cx<T>* z, double conv, int max_iter, int* it,
-               cx<T>* out) {
+               cx<T>* out, long long ss = 0, int period = 1, int lds = 0) {
+    if (lds <= 0) lds = m;
     const int ld = L.m;
     const long long sm = (long long)L.mat;
     cx<T>* al = w.mats[0];
@@ -441,10 +592,10 @@ struct Engine {
     cx<T>* aln = w.mats[8];
     cx<T>* ben = w.mats[9];
     const cx<T> one = hc<T>(1.0), zero = hc<T>(0.0);
-    k_copy<T><<<eg(m * m), 256, 0, s>>>(e1, sm, h00, 0, m, m, m, ld, 0);
-    k_copy<T><<<eg(m * m), 256, 0, s>>>(es, sm, h00, 0, m, m, m, ld, 0);
-    k_copy<T><<<eg(m * m), 256, 0, s>>>(al, sm, v, 0, m, m, m, ld, 1);
-    k_copy<T><<<eg(m * m), 256, 0, s>>>(be, sm, v, 0, m, m, m, ld, 0);
+    k_copy_per<T><<<eg(m * m), 256, 0, s>>>(e1, sm, h00, ss, period, lds, m, m, ld, 0);
+    k_copy_per<T><<<eg(m * m), 256, 0, s>>>(es, sm, h00, ss, period, lds, m, m, ld, 0);
+    k_copy_per<T><<<eg(m * m), 256, 0, s>>>(al, sm, v, ss, period, lds, m, m, ld, 1);
+    k_copy_per<T><<<eg(m * m), 256, 0, s>>>(be, sm, v, ss, period, lds, m, m, ld, 0);
     k_fill<<<(B + 255) / 256, 256, 0, s>>>(it, B, 0);
     k_fill<<<(B + 255) / 256, 256, 0, s>>>(w.active, B, 1);
     TL_CUDA(cudaGetLastError());
@@ -475,6 +626,33 @@ struct Engine {
     return inverse(out, m, nullptr);
   }
 
+  // Surface Green's function of one lead, g = inv(z - es) into out: the
+  // decimation of the full matrices, or with block-circulant leads
+  // circular_g (negf/circular.f90:42-105): transform, decimate the K small
+  // blocks of every point as one batch of B K, transform back.
+  int lead(int m, const cx<T>* h00, const cx<T>* v, const cx<T>* z, double conv, int max_iter, int* it, cx<T>* out,
+           const double* gr_fwd) {
+    if (!circ || circ->K() == 1) return decimate(m, h00, v, z, conv, max_iter, it, out);
+    const int ny = circ->ny, nx = circ->nx, K = circ->K(), sb = m / K;
+    Engine<T>& e = *small;
+    e.B = B * K;
+    const long long s2 = (long long)sb * sb;
+    cx<T>* hs = e.w.mats[12];
+    cx<T>* vs = e.w.mats[13];
+    cx<T>* gs = e.w.mats[10];
+    k_circ_fwd<T><<<dim3((unsigned)((s2 + 255) / 256), K), 256, 0, s>>>(h00, v, m, ny, nx, gr_fwd[0], gr_fwd[1], hs,
+                                                                        vs);
+    k_circ_points<T><<<(B * K + 255) / 256, 256, 0, s>>>(z, B, K, e.w.zl, e.w.st);
+    TL_CUDA(cudaGetLastError());
+    int rc = e.decimate(sb, hs, vs, e.w.zl, conv, max_iter, e.w.itl, gs, s2, K, sb);
+    if (rc) return rc;
+    k_circ_fold<<<(B + 255) / 256, 256, 0, s>>>(e.w.itl, e.w.st, B, K, it, w.st);
+    k_circ_back<T><<<eg(m * m), 256, 0, s>>>(out, (long long)L.mat, L.m, gs, m, ny, nx, circ->gr_l[0],
+                                             circ->gr_l[1]);
+    TL_CUDA(cudaGetLastError());
+    return PF_SUCCESS;
+  }
+
   // One batch of points sharing block set q: leads, sweep, Caroli.
   int run(const pf::System<T>& sys, int q, const double* E, int cnt, double eta, double eta0, double devf,
           double conv, int max_iter, bool mirror, const int* zero_flag, double* transl, int* status, int* iters) {
@@ -502,7 +680,7 @@ struct Engine {
     cx<T>* t2 = w.mats[2];
     int rc;
     // ---- left lead, advanced: z = E - i eps, alpha0 = Hlv^H, beta0 = Hlv
-    if ((rc = decimate(nl, HL, HLv, w.zl, conv, max_iter, w.itl, t1))) return rc;
+    if ((rc = lead(nl, HL, HLv, w.zl, conv, max_iter, w.itl, t1, circ ? circ->gr_l : nullptr))) return rc;
     TL_CUDA(gemm(nl, nl, nl, t1, ld, sm, false, HLv, nl, 0, false, t0, ld, sm, one, zero, nullptr));  // g V
     TL_CUDA(gemm(nl, nl, nl, HLv, nl, 0, true, t0, ld, sm, false, t2, ld, sm, one, zero, nullptr));   // sl_adv
     // wrapper conversions (lesser.f90:141-144): gl = gl_adv^H, sl = sl_adv^H, gml = -gml_adv
@@ -518,7 +696,7 @@ struct Engine {
       k_copy<T><<<eg(nr * nr), 256, 0, s>>>(gmr, sm, gml, sm, ld, nr, nr, ld, 0);
       TL_CUDA(cudaMemcpyAsync(w.itr, w.itl, sizeof(int) * B, cudaMemcpyDeviceToDevice, s));
     } else {
-      if ((rc = decimate(nr, HR, HRv, w.zr, conv, max_iter, w.itr, gr))) return rc;
+      if ((rc = lead(nr, HR, HRv, w.zr, conv, max_iter, w.itr, gr, circ ? circ->gr_r : nullptr))) return rc;
       TL_CUDA(gemm(nr, nr, nr, gr, ld, sm, false, HRv, nr, 0, false, t0, ld, sm, one, zero, nullptr));
       TL_CUDA(gemm(nr, nr, nr, HRv, nr, 0, true, t0, ld, sm, false, sr, ld, sm, one, zero, nullptr));
       k_gamma<T><<<eg(nr * nr), 256, 0, s>>>(gmr, sr, sm, nr, ld, 1);
@@ -575,13 +753,19 @@ template <typename T>
 int drive(int n, int nl, int nr, int L, int nq, const double* const blk[8], int npts, const double* E,
           const int* qidx, const int* zero_flag, double eta, double eta0, double dev_factor, double convergence,
           int max_iter, double* transl, int* status, int* iters, char* base, size_t work_bytes, cudaStream_t st,
-          int arith) {
+          int arith, const Circ* circ) {
   Engine<T> e;
   const bool tc = arith == PF_ARITH_TC;
-  e.L = tlayout(n, nl, nr, npts, sizeof(cx<T>), tc);
+  const int K = circ ? circ->K() : 1;
+  e.L = tiled_layout(n, nl, nr, npts, sizeof(cx<T>), tc, K);
   const size_t cb = conv_bytes(n, nl, nr, L, arith);
   const size_t tcb = tc ? pf::tc::zgemm_workspace(e.L.m, e.L.m, e.L.m, e.L.batch, false, false) : 0;
-  const size_t need = 256 + cb + carve<T>(nullptr, e.L, &e.w) + tcb;
+  size_t need = 256 + cb + carve<T>(nullptr, e.L, &e.w) + tcb;
+  Engine<T> se;  // small blocks of block-circulant leads
+  if (K > 1) {
+    se.L = small_layout(e.L, K, sizeof(cx<T>));
+    need += round256(tcb) - tcb + carve<T>(nullptr, se.L, &se.w);
+  }
   if (!base || work_bytes < need) return set_err(PF_ERR_ARG, "pf_tiled: workspace too small");
   if (tc && !pf::tc::tma_available())
     return set_err(PF_ERR_CUDA, "pf_tiled: the driver provides no cuTensorMapEncodeTiled");
@@ -598,6 +782,13 @@ int drive(int n, int nl, int nr, int L, int nq, const double* const blk[8], int 
   e.s = st;
   int host_count = 0;
   e.host_count = &host_count;
+  if (K > 1) {
+    carve<T>(base + 256 + cb + wb + round256(tcb), se.L, &se.w);
+    se.s = st;
+    se.host_count = &host_count;
+    e.circ = circ;
+    e.small = &se;
+  }
   std::vector<int> q(npts, 0);
   if (qidx) {
     TL_CUDA(cudaStreamSynchronize(st));
@@ -677,6 +868,62 @@ int drive(int n, int nl, int nr, int L, int nq, const double* const blk[8], int 
   return PF_SUCCESS;
 }
 
+size_t tiled_bytes(int n, int nl, int nr, int L, int nq, int npts, int arith, int K) {
+  if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0) return 0;
+  if (n > PF_NMAX_TILED || nl > PF_NMAX_TILED || nr > PF_NMAX_TILED) return 0;
+  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64 && arith != PF_ARITH_TC) return 0;
+  const TLayout L2 = tiled_layout(n, nl, nr, npts, 16, arith == PF_ARITH_TC, K);
+  const size_t cb = conv_bytes(n, nl, nr, L, arith);
+  const size_t tcb = arith == PF_ARITH_TC ? pf::tc::zgemm_workspace(L2.m, L2.m, L2.m, L2.batch, false, false) : 0;
+  size_t b = 256 + cb + tcb;
+  if (arith != PF_ARITH_DF64) {
+    Work<double> w;
+    b += carve<double>(nullptr, L2, &w);
+  } else {
+    Work<pf::df64> w;
+    b += carve<pf::df64>(nullptr, L2, &w);
+  }
+  if (K > 1) {
+    const TLayout S = small_layout(L2, K, 16);
+    Work<double> w;  // complex double and complex double-float have the same size
+    b += round256(tcb) - tcb + carve<double>(nullptr, S, &w);
+  }
+  return b;
+}
+
+// nullptr when (nl, nr, ny, nx) describe block-circulant leads
+const char* circ_dims_error(int nl, int nr, int ny, int nx) {
+  if (ny < 1 || nx < 1) return "pf_tiled_circ: n_bloch_y and n_bloch_x must be positive";
+  if ((long long)ny * nx > 256) return "pf_tiled_circ: at most 256 Bloch cells";
+  if (nl != nr) return "pf_tiled_circ: block-circulant leads need nl == nr";
+  if (nl <= 0 || nl % (ny * nx)) return "pf_tiled_circ: nl must be a multiple of n_bloch_y * n_bloch_x";
+  return nullptr;
+}
+
+int tiled_entry(int n, int nl, int nr, int L, int nq, const double* const blk[8], int npts, const double* E,
+                const int* qidx, const int* zero_flag, double eta, double eta0, double dev_factor, double convergence,
+                int max_iter, int arith, const Circ* circ, double* transl, int* status, int* iters, void* work,
+                size_t work_bytes, void* stream) {
+  if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0)
+    return set_err(PF_ERR_ARG, "pf_tiled: dimensions must be positive");
+  if (n > PF_NMAX_TILED || nl > PF_NMAX_TILED || nr > PF_NMAX_TILED)
+    return set_err(PF_ERR_SIZE, "pf_tiled: block size exceeds PF_NMAX_TILED");
+  for (int k = 0; k < 8; ++k)
+    if (!blk[k] && !(k == 5 && L == 1)) return set_err(PF_ERR_ARG, "pf_tiled: null block pointer");
+  if (!E || !transl || !status) return set_err(PF_ERR_ARG, "pf_tiled: null pointer");
+  if (max_iter <= 0) return set_err(PF_ERR_ARG, "pf_tiled: max_iter must be positive");
+  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64 && arith != PF_ARITH_TC)
+    return set_err(PF_ERR_ARG, "pf_tiled: unknown arithmetic");
+  if (npts == 0) return PF_SUCCESS;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* base = reinterpret_cast<char*>(work);
+  if (arith != PF_ARITH_DF64)
+    return drive<double>(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence,
+                         max_iter, transl, status, iters, base, work_bytes, st, arith, circ);
+  return drive<pf::df64>(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence,
+                         max_iter, transl, status, iters, base, work_bytes, st, arith, circ);
+}
+
 }  // namespace
 
 extern "C" {
@@ -704,19 +951,7 @@ int pf_tiled_layout(int n, int nl, int nr, int npts, int arith, int* panel, int*
 }
 
 size_t pf_transport_tdb_tiled_workspace_size(int n, int nl, int nr, int L, int nq, int npts, int arith) {
-  if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0) return 0;
-  if (n > PF_NMAX_TILED || nl > PF_NMAX_TILED || nr > PF_NMAX_TILED) return 0;
-  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64 && arith != PF_ARITH_TC) return 0;
-  const TLayout L2 = tlayout(n, nl, nr, npts, 16, arith == PF_ARITH_TC);
-  const size_t cb = conv_bytes(n, nl, nr, L, arith);
-  if (arith != PF_ARITH_DF64) {
-    Work<double> w;
-    const size_t tcb =
-        arith == PF_ARITH_TC ? pf::tc::zgemm_workspace(L2.m, L2.m, L2.m, L2.batch, false, false) : 0;
-    return 256 + cb + carve<double>(nullptr, L2, &w) + tcb;
-  }
-  Work<pf::df64> w;
-  return 256 + cb + carve<pf::df64>(nullptr, L2, &w);
+  return tiled_bytes(n, nl, nr, L, nq, npts, arith, 1);
 }
 
 int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
@@ -725,25 +960,38 @@ int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq, const doubl
                                const int* zero_flag, double eta, double eta0, double dev_factor, double convergence,
                                int max_iter, int arith, double* transl, int* status, int* iters, void* work,
                                size_t work_bytes, void* stream) {
-  if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0)
-    return set_err(PF_ERR_ARG, "pf_tiled: dimensions must be positive");
-  if (n > PF_NMAX_TILED || nl > PF_NMAX_TILED || nr > PF_NMAX_TILED)
-    return set_err(PF_ERR_SIZE, "pf_tiled: block size exceeds PF_NMAX_TILED");
-  if (!HL || !HLv || !HR || !HRv || !Hd || !Hld || !Hrd || (L > 1 && !Hdv))
-    return set_err(PF_ERR_ARG, "pf_tiled: null block pointer");
-  if (!E || !transl || !status) return set_err(PF_ERR_ARG, "pf_tiled: null pointer");
-  if (max_iter <= 0) return set_err(PF_ERR_ARG, "pf_tiled: max_iter must be positive");
-  if (arith != PF_ARITH_FP64 && arith != PF_ARITH_DF64 && arith != PF_ARITH_TC)
-    return set_err(PF_ERR_ARG, "pf_tiled: unknown arithmetic");
-  if (npts == 0) return PF_SUCCESS;
   const double* blk[8] = {HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd};
-  cudaStream_t st = (cudaStream_t)stream;
-  char* base = reinterpret_cast<char*>(work);
-  if (arith != PF_ARITH_DF64)
-    return drive<double>(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence,
-                         max_iter, transl, status, iters, base, work_bytes, st, arith);
-  return drive<pf::df64>(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence,
-                         max_iter, transl, status, iters, base, work_bytes, st, arith);
+  return tiled_entry(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence, max_iter,
+                     arith, nullptr, transl, status, iters, work, work_bytes, stream);
+}
+
+size_t pf_transport_tdb_tiled_circ_workspace_size(int n, int nl, int nr, int L, int nq, int npts, int arith,
+                                                  int n_bloch_y, int n_bloch_x) {
+  if (circ_dims_error(nl, nr, n_bloch_y, n_bloch_x)) return 0;
+  return tiled_bytes(n, nl, nr, L, nq, npts, arith, n_bloch_y * n_bloch_x);
+}
+
+int pf_transport_tdb_tiled_circ_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
+                                    const double* HR, const double* HRv, const double* Hd, const double* Hdv,
+                                    const double* Hld, const double* Hrd, int npts, const double* E,
+                                    const int* qidx, const int* zero_flag, double eta, double eta0,
+                                    double dev_factor, double convergence, int max_iter, int arith, int n_bloch_y,
+                                    int n_bloch_x, const double* gr, double* transl, int* status, int* iters,
+                                    void* work, size_t work_bytes, void* stream) {
+  if (const char* why = circ_dims_error(nl, nr, n_bloch_y, n_bloch_x)) return set_err(PF_ERR_ARG, why);
+  if (!gr) return set_err(PF_ERR_ARG, "pf_tiled_circ: null gr");
+  Circ c;
+  c.ny = n_bloch_y;
+  c.nx = n_bloch_x;
+  c.gr_l[0] = gr[0];
+  c.gr_l[1] = gr[1];
+  c.gr_r[0] = gr[2];
+  c.gr_r[1] = gr[3];
+  for (int i = 0; i < 4; ++i)
+    if (!std::isfinite(gr[i])) return set_err(PF_ERR_ARG, "pf_tiled_circ: gr must be finite");
+  const double* blk[8] = {HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd};
+  return tiled_entry(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence, max_iter,
+                     arith, &c, transl, status, iters, work, work_bytes, stream);
 }
 
 }  // extern "C"

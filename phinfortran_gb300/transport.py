@@ -85,13 +85,27 @@ NMAX_RESIDENT = 48   # PF_NMAX_RESIDENT
 TILED_ARITH = {"fp64": 0, "df64": 1, "tc": 2, "mixed": 2}
 
 
+def _circular_args(circular, nl, nr):
+    """(n_bloch_y, n_bloch_x, gr[4]) of the block-circulant lead option."""
+    if isinstance(circular, dict):
+        ny, nx, gr = circular["n_bloch_y"], circular["n_bloch_x"], circular["gr"]
+    else:
+        ny, nx, gr = circular
+    gr = np.ascontiguousarray(np.broadcast_to(np.asarray(gr, dtype=np.float64), (4,)))
+    ny, nx = int(ny), int(nx)
+    if ny < 1 or nx < 1 or nl != nr or nl % (ny * nx):
+        raise ValueError("block-circulant leads need nl == nr, a multiple of n_bloch_y * n_bloch_x")
+    return ny, nx, gr
+
+
 def _transport_tiled(E, nq, dims, arrs, *, eta, eta0, convergence, dev_factor, qidx, zero_flag, max_iter,
-                     want_transr, check, precision):
+                     want_transr, check, precision, circular=None):
     """Blocks above the resident size: pf_transport_tdb_tiled_dev on torch
     device buffers (T_L only).  precision: "fp64" (SIMT FP64 block
     products), "tc" (the FP64 algorithm with every block product on the
     tensor cores as exact BF16 slice products), "df64" (double-float
-    arithmetic on the FP32 pipe, ~48-bit); "mixed" selects "tc"."""
+    arithmetic on the FP32 pipe, ~48-bit); "mixed" selects "tc".
+    circular: block-circulant leads (pf_transport_tdb_tiled_circ_dev)."""
     import torch
     if want_transr:
         raise ValueError("T_R is not computed for blocks above 48 (pass want_transr=False)")
@@ -107,15 +121,24 @@ def _transport_tiled(E, nq, dims, arrs, *, eta, eta0, convergence, dev_factor, q
     tl = torch.zeros(max(npts, 1), dtype=torch.float64, device="cuda")
     st = torch.zeros(max(npts, 1), dtype=torch.int32, device="cuda")
     it = torch.zeros((max(npts, 1), 2), dtype=torch.int32, device="cuda")
-    ws = lib.pf_transport_tdb_tiled_workspace_size(n, nl, nr, L, nq, npts, arith)
-    if ws == 0:
-        _abi.check(-3)
-    work = torch.empty(ws, dtype=torch.uint8, device="cuda")
     p = lambda t: None if t is None else t.data_ptr()
-    rc = lib.pf_transport_tdb_tiled_dev(n, nl, nr, L, nq, *[dev[k].data_ptr() for k in BLOCK_NAMES], npts,
-                                        Ed.data_ptr(), p(qd), p(zd), eta, eta0, dev_factor, convergence, max_iter,
-                                        arith, tl.data_ptr(), st.data_ptr(), it.data_ptr(), work.data_ptr(), ws,
-                                        C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    head = (n, nl, nr, L, nq, *[dev[k].data_ptr() for k in BLOCK_NAMES], npts, Ed.data_ptr(), p(qd), p(zd), eta,
+            eta0, dev_factor, convergence, max_iter, arith)
+    outs = (tl.data_ptr(), st.data_ptr(), it.data_ptr())
+    if circular is None:
+        ws = lib.pf_transport_tdb_tiled_workspace_size(n, nl, nr, L, nq, npts, arith)
+        if ws == 0:
+            _abi.check(-3)
+        work = torch.empty(ws, dtype=torch.uint8, device="cuda")
+        rc = lib.pf_transport_tdb_tiled_dev(*head, *outs, work.data_ptr(), ws, stream)
+    else:
+        ny, nx, gr = _circular_args(circular, nl, nr)
+        ws = lib.pf_transport_tdb_tiled_circ_workspace_size(n, nl, nr, L, nq, npts, arith, ny, nx)
+        if ws == 0:
+            _abi.check(-3)
+        work = torch.empty(ws, dtype=torch.uint8, device="cuda")
+        rc = lib.pf_transport_tdb_tiled_circ_dev(*head, ny, nx, _ptr(gr), *outs, work.data_ptr(), ws, stream)
     if rc != 0:
         raise _abi.PFError(rc, lib.pf_tiled_last_error().decode(errors="replace"))
     torch.cuda.synchronize()
@@ -127,7 +150,7 @@ def _transport_tiled(E, nq, dims, arrs, *, eta, eta0, convergence, dev_factor, q
 
 def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=None,
                   zero_flag=None, max_iter=1000, want_transr=True, check=True,
-                  precision="fp64", refine_iters=2):
+                  precision="fp64", refine_iters=2, circular=None):
     """Transmission for a batch of points through the host-pointer C entry.
 
     E: (npts,) energies (omega^2 for phonons).  blocks: TdbBlocks or dict.
@@ -141,6 +164,11 @@ def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=No
     Blocks above 48 go through the large-block entry, where "mixed" (or
     "tc") puts the block products on the tensor cores and "df64" selects
     the double-float engine.
+    circular: block-circulant leads (the reference's circular_flag = 1),
+    (n_bloch_y, n_bloch_x, gr) or a dict with those keys, gr = the G.R
+    products {left y, left x, right y, right x}; the lead surface Green's
+    functions then come from circular_g (negf/circular.f90:42-105) on the
+    large-block engine, at any block size, with T_L only.
     Returns dict(transl, transr, status, iters).
     """
     if precision not in TILED_ARITH:
@@ -149,12 +177,12 @@ def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=No
     if isinstance(blocks, dict):
         blocks = TdbBlocks.from_dict(blocks)
     nq, (n, nl, nr, L), arrs = blocks.stacked()
-    if max(n, nl, nr) <= NMAX_RESIDENT and precision in ("tc", "df64"):
+    if max(n, nl, nr) <= NMAX_RESIDENT and precision in ("tc", "df64") and circular is None:
         raise ValueError("precision 'tc' and 'df64' are large-block (n > 48) arithmetics")
-    if max(n, nl, nr) > NMAX_RESIDENT:
+    if max(n, nl, nr) > NMAX_RESIDENT or circular is not None:
         return _transport_tiled(E, nq, (n, nl, nr, L), arrs, eta=eta, eta0=eta0, convergence=convergence,
                                 dev_factor=dev_factor, qidx=qidx, zero_flag=zero_flag, max_iter=max_iter,
-                                want_transr=want_transr, check=check, precision=precision)
+                                want_transr=want_transr, check=check, precision=precision, circular=circular)
     buf = {k: fortran_block(v) for k, v in arrs.items()}
     E = np.ascontiguousarray(E, dtype=np.float64)
     npts = E.shape[0]

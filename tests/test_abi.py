@@ -127,3 +127,27 @@ def test_tiled_tuning_knobs_without_gpu(built_lib):
         assert p.value == 32 and b.value == 256
     finally:
         lib.pf_tiled_set_tuning(0, 0)
+
+
+def test_tiled_circular_validation_without_gpu(built_lib):
+    """The block-circulant entry checks its Bloch cells on the host: nl must
+    equal nr and be a multiple of n_bloch_y * n_bloch_x, gr must be given;
+    its workspace is the plain engine's plus the small-block engine's."""
+    import ctypes as C
+
+    from phinfortran_gb300 import _abi
+    lib = _abi.load()
+    ws = lib.pf_transport_tdb_tiled_circ_workspace_size
+    plain = lib.pf_transport_tdb_tiled_workspace_size(96, 96, 96, 10, 1, 64, 0)
+    assert ws(96, 96, 96, 10, 1, 64, 0, 2, 2) > plain
+    assert ws(96, 96, 96, 10, 1, 64, 0, 5, 2) == 0
+    assert ws(96, 96, 48, 10, 1, 64, 0, 2, 2) == 0
+    assert ws(96, 96, 96, 10, 1, 64, 0, 0, 2) == 0
+    gr = (C.c_double * 4)(*([6.283185307179586] * 4))
+    args = [96, 96, 96, 10, 1] + [None] * 8 + [1, None, None, None, 0.0, 1e-5, 10.0, 1e-14, 100, 0]
+    rc = lib.pf_transport_tdb_tiled_circ_dev(*args, 5, 2, gr, None, None, None, None, 0, None)
+    assert rc == -1 and b"multiple" in lib.pf_tiled_last_error()
+    rc = lib.pf_transport_tdb_tiled_circ_dev(*args, 2, 2, None, None, None, None, None, 0, None)
+    assert rc == -1 and b"gr" in lib.pf_tiled_last_error()
+    rc = lib.pf_transport_tdb_tiled_circ_dev(*args, 2, 2, gr, None, None, None, None, 0, None)
+    assert rc == -1 and b"null block pointer" in lib.pf_tiled_last_error()
