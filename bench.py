@@ -216,13 +216,16 @@ def time_steps(torch, fn, steps, flush, stream):
     return times
 
 
-def large_block_sample(torch, sizes=((2, 8, 32), (3, 8, 20), (4, 2, 4))):
+def large_block_sample(torch, sizes=((2, 2, 128), (3, 2, 128), (4, 1, 32)), extras=True):
     """Large-block engine on diamond-slab stacks (first + second neighbour
     springs, 28 / 72.6 mass blocks of 10 layers, L = 60): the plain FP64
     path (SIMT FP64 block products), the tensor-core path (the same FP64
     algorithm with every block product on tcgen05 as exact BF16 slice
-    products) and the double-float engine, on n = 96 (8 transverse k x 32
-    omega), n = 216 (8 x 20) and n = 384 (2 x 4)."""
+    products) and the double-float engine.  Each sample keeps the shape of
+    the 64 q x 512 omega workload -- many frequencies per transverse k, so
+    that the per-q batches of the engine fill the GPU -- at a size that runs
+    in seconds: n = 96 (2 transverse k x 128 omega), n = 216 (2 x 128) and
+    n = 384 (1 x 32)."""
     from phinfortran_gb300 import systems as S, transport_tdb
     out = []
     for nc, nk, ne in sizes:
@@ -257,7 +260,7 @@ def large_block_sample(torch, sizes=((2, 8, 32), (3, 8, 20), (4, 2, 4))):
                         status_nonzero={k: int((res[k][1]["status"] != 0).sum()) for k in res},
                         note="host-pointer call (blocks copied to the device inside the timed region); "
                              "deviation = max |T - T64| / max(|T64|, 1e-3); built-in panel width and batch"))
-        if n == 216:
+        if n == 216 and extras:
             # the autotuner on a 48-point subsample of this problem (tensor-core
             # arithmetic): panel width of the blocked inverse x batch
             import tempfile
@@ -271,7 +274,8 @@ def large_block_sample(torch, sizes=((2, 8, 32), (3, 8, 20), (4, 2, 4))):
                                        tuned_s=best["seconds"], default_s=best["default_seconds"],
                                        candidates=[(c["panel"], c["batch"], c["seconds"]) for c in best["candidates"]],
                                        note="panel 0 / batch 0 = the built-in choice")
-    out.append(circular_sample(torch))
+    if extras:
+        out.append(circular_sample(torch))
     return out
 
 
