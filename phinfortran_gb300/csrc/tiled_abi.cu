@@ -329,6 +329,57 @@ __global__ void k_circ_back(cx<T>* out, long long so, int ld, const cx<T>* gs, i
   }
   out[(size_t)b * so + R + (size_t)Cc * ld] = pf::mk<T>(T(xr / K), T(xi / K));
 }
+// Small decimations of block-circulant leads with blocks of at most 48: the
+// resident FP64 decimation of the n <= 48 kernels (transport.cuh), one CTA
+// a small block with its matrices in shared memory, a persistent grid over
+// the B K blocks; g = inv(z - es) of block i into gs + i s^2 (ld s).
+constexpr int kCircThreads = 256;
+constexpr int kCircGridCap = 1024;  // CTAs in flight: bounds the global scratch
+struct CircLayout {
+  int m, ld;
+  size_t mat, smem;
+};
+inline CircLayout circ_layout(int s) {
+  CircLayout l;
+  l.m = s;
+  l.ld = s | 1;
+  l.mat = (size_t)l.ld * s;
+  l.smem = pf::NSM * l.mat * 16 + 32 * sizeof(double) + 2 * (size_t)s * 16 + (size_t)s * sizeof(int) + 64 * sizeof(int);
+  return l;
+}
+template <int S>
+__global__ void __launch_bounds__(kCircThreads)
+    k_circ_decimate(const cx<double>* hs, const cx<double>* vs, int K, int total, const cx<double>* z, double conv,
+                    int max_iter, cx<double>* gs, int* it_s, int* st_s, char* gscr, CircLayout lay) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int s = lay.m;
+  pf::Ctx<double> c;
+  cx<double>* sm = reinterpret_cast<cx<double>*>(smem_raw);
+  for (int i = 0; i < pf::NSM; ++i) c.sm[i] = sm + i * lay.mat;
+  unsigned char* tail = reinterpret_cast<unsigned char*>(sm + pf::NSM * lay.mat);
+  c.red = reinterpret_cast<double*>(tail);
+  c.iw.rowk = reinterpret_cast<cx<double>*>(tail + 32 * sizeof(double));
+  c.iw.colk = c.iw.rowk + s;
+  int* ip = reinterpret_cast<int*>(c.iw.colk + s);
+  c.iw.perm = ip;
+  c.iw.flag = ip + s;
+  cx<double>* g = reinterpret_cast<cx<double>*>(gscr) + (size_t)blockIdx.x * pf::NG * lay.mat;
+  for (int i = 0; i < pf::NG; ++i) c.gs[i] = g + i * lay.mat;
+  c.ld = lay.ld;
+  for (int i = blockIdx.x; i < total; i += gridDim.x) {
+    const size_t kb = (size_t)(i % K) * s * s;
+    int it = 0;
+    // alpha = vs^H, beta = vs (util.f90 decimation: beta = alpha^H)
+    const int st = pf::decimate<double, S>(c, s, z[i / K], pf::opN<double>(hs + kb, s), pf::opC<double>(vs + kb, s),
+                                           pf::opN<double>(vs + kb, s), conv, max_iter, &it);
+    pf::copy_out(gs + (size_t)i * s * s, s, false, c.sm[2], c.ld, s, s);
+    if (threadIdx.x == 0) {
+      it_s[i] = it;
+      st_s[i] = st;
+    }
+    __syncthreads();
+  }
+}
 // zs[b K + k] = z[b]; st_s = 0
 template <typename T>
 __global__ void k_circ_points(const cx<T>* z, int B, int K, cx<T>* zs, int* st_s) {
@@ -390,6 +441,13 @@ TLayout tlayout(int n, int nl, int nr, int npts, size_t cxb, bool tc = false) {
   if (npts > 0 && (size_t)npts < b) b = npts;
   l.batch = (int)b;
   return l;
+}
+
+// global scratch of the resident small decimations (0: blocks above 48,
+// which go through the batched small-block engine)
+size_t circ_scratch_bytes(int sb) {
+  if (sb > PF_NMAX_RESIDENT) return 0;
+  return round256((size_t)kCircGridCap * pf::NG * circ_layout(sb).mat * 16);
 }
 
 // tlayout with the batch bounded so that the small-block batch of
@@ -470,6 +528,7 @@ struct Engine {
   // (batch B K, FP64 or double-float SIMT products)
   const Circ* circ = nullptr;
   Engine<T>* small = nullptr;
+  char* circ_scr = nullptr;  // scratch of the resident small decimations (FP64, blocks <= 48)
 
   dim3 eg(int elems) const { return dim3((elems + 255) / 256, B); }
 
@@ -642,10 +701,31 @@ struct Engine {
     cx<T>* gs = e.w.mats[10];
     k_circ_fwd<T><<<dim3((unsigned)((s2 + 255) / 256), K), 256, 0, s>>>(h00, v, m, ny, nx, gr_fwd[0], gr_fwd[1], hs,
                                                                         vs);
-    k_circ_points<T><<<(B * K + 255) / 256, 256, 0, s>>>(z, B, K, e.w.zl, e.w.st);
     TL_CUDA(cudaGetLastError());
-    int rc = e.decimate(sb, hs, vs, e.w.zl, conv, max_iter, e.w.itl, gs, s2, K, sb);
-    if (rc) return rc;
+    bool resident = false;
+    if constexpr (std::is_same<T, double>::value) resident = circ_scr != nullptr;
+    if (resident) {
+      if constexpr (std::is_same<T, double>::value) {
+        const CircLayout cl = circ_layout(sb);
+        const int Sx = (sb + 31) / 32;
+        auto kfn = Sx == 1 ? k_circ_decimate<1> : k_circ_decimate<2>;
+        TL_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl.smem));
+        int per_sm = 0, dev = 0, sms = 0;
+        TL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kCircThreads, cl.smem));
+        TL_CUDA(cudaGetDevice(&dev));
+        TL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        if (per_sm < 1) return set_err(PF_ERR_SIZE, "pf_tiled_circ: small decimation does not fit on the device");
+        const int grid = std::min(std::min(B * K, sms * per_sm), kCircGridCap);
+        kfn<<<grid, kCircThreads, cl.smem, s>>>(hs, vs, K, B * K, z, conv, max_iter, gs, e.w.itl, e.w.st, circ_scr,
+                                                cl);
+        TL_CUDA(cudaGetLastError());
+      }
+    } else {
+      k_circ_points<T><<<(B * K + 255) / 256, 256, 0, s>>>(z, B, K, e.w.zl, e.w.st);
+      TL_CUDA(cudaGetLastError());
+      int rc = e.decimate(sb, hs, vs, e.w.zl, conv, max_iter, e.w.itl, gs, s2, K, sb);
+      if (rc) return rc;
+    }
     k_circ_fold<<<(B + 255) / 256, 256, 0, s>>>(e.w.itl, e.w.st, B, K, it, w.st);
     k_circ_back<T><<<eg(m * m), 256, 0, s>>>(out, (long long)L.mat, L.m, gs, m, ny, nx, circ->gr_l[0],
                                              circ->gr_l[1]);
@@ -762,9 +842,12 @@ int drive(int n, int nl, int nr, int L, int nq, const double* const blk[8], int 
   const size_t tcb = tc ? pf::tc::zgemm_workspace(e.L.m, e.L.m, e.L.m, e.L.batch, false, false) : 0;
   size_t need = 256 + cb + carve<T>(nullptr, e.L, &e.w) + tcb;
   Engine<T> se;  // small blocks of block-circulant leads
+  size_t scr = 0;
   if (K > 1) {
     se.L = small_layout(e.L, K, sizeof(cx<T>));
     need += round256(tcb) - tcb + carve<T>(nullptr, se.L, &se.w);
+    if (std::is_same<T, double>::value) scr = circ_scratch_bytes(nl / K);
+    need += scr;
   }
   if (!base || work_bytes < need) return set_err(PF_ERR_ARG, "pf_tiled: workspace too small");
   if (tc && !pf::tc::tma_available())
@@ -783,7 +866,8 @@ int drive(int n, int nl, int nr, int L, int nq, const double* const blk[8], int 
   int host_count = 0;
   e.host_count = &host_count;
   if (K > 1) {
-    carve<T>(base + 256 + cb + wb + round256(tcb), se.L, &se.w);
+    const size_t sw = carve<T>(base + 256 + cb + wb + round256(tcb), se.L, &se.w);
+    if (scr) e.circ_scr = base + 256 + cb + wb + round256(tcb) + sw;
     se.s = st;
     se.host_count = &host_count;
     e.circ = circ;
@@ -887,6 +971,7 @@ size_t tiled_bytes(int n, int nl, int nr, int L, int nq, int npts, int arith, in
     const TLayout S = small_layout(L2, K, 16);
     Work<double> w;  // complex double and complex double-float have the same size
     b += round256(tcb) - tcb + carve<double>(nullptr, S, &w);
+    if (arith != PF_ARITH_DF64) b += circ_scratch_bytes(nl / K);
   }
   return b;
 }

@@ -2,6 +2,7 @@
 
     python -m phinfortran_gb300.run ribbon   --energies 64 --precision mixed
     python -m phinfortran_gb300.run diamond  --nc 3 --layers 4 --kpoints 2 --energies 8
+    python -m phinfortran_gb300.run diamond  --nc 3 --layers 10 --energies 96 --circular --precision tc
     python -m phinfortran_gb300.run ribbon3  --width 256 --layers 1000 --energies 4 --perturb 1e-15
     python -m phinfortran_gb300.run sc       --layers 40 --energies 64 --mode grad --arith df64
     python -m phinfortran_gb300.run sisi     --kpoints 1 --energies 16 --mode modes
@@ -41,7 +42,12 @@ def _build(a):
         return b, E[sel], p, dict(aux, sel=sel)
     if a.workload == "diamond":
         kp = list(range(0, 64, max(1, 64 // a.kpoints)))[:a.kpoints]
-        b, E, p, aux = S.diamond_phonon(nc=a.nc, L=a.layers or 60, kpoints=kp)
+        if a.gamma or a.circular:
+            # the transverse Gamma point (block-circulant leads), one block set
+            kp = [0]
+            b, E, p, aux = S.diamond_phonon(nc=a.nc, L=a.layers or 60, nk_side=1)
+        else:
+            b, E, p, aux = S.diamond_phonon(nc=a.nc, L=a.layers or 60, kpoints=kp)
         Es = E[np.linspace(10, 500, a.energies).astype(int)]
         q = np.repeat(np.arange(len(kp), dtype=np.int32), Es.size)
         return b, np.tile(Es, len(kp)), p, dict(qidx=q)
@@ -63,6 +69,10 @@ def main():
     ap.add_argument("--width", type=int, default=0)
     ap.add_argument("--nc", type=int, default=2)
     ap.add_argument("--perturb", type=float, default=0.0)
+    ap.add_argument("--gamma", action="store_true", help="diamond: the transverse Gamma point only")
+    ap.add_argument("--circular", action="store_true",
+                    help="diamond at the transverse Gamma point with the block-circulant lead option "
+                         "(circular_flag = 1, nc x nc Bloch cells)")
     ap.add_argument("--out", default="",
                     help="sisi: write the reference's ten output tables and the per-k mode files into this directory")
     a = ap.parse_args()
@@ -131,7 +141,9 @@ def main():
                    status=int(np.bitwise_or.reduce(st)))
     else:
         from .transport import transport_tdb
-        r = transport_tdb(E, b, qidx=qidx, want_transr=False, check=False, precision=a.precision, **p)
+        circ = (a.nc, a.nc, [2.0 * np.pi] * 4) if (a.circular and a.workload == "diamond") else None
+        r = transport_tdb(E, b, qidx=qidx, want_transr=False, check=False, precision=a.precision, circular=circ,
+                          **p)
         torch.cuda.synchronize()
         out.update(points=int(E.size), seconds=time.perf_counter() - t0, transl=r["transl"].tolist(),
                    iters=r["iters"][:, 0].tolist(), status=int(np.bitwise_or.reduce(r["status"])))

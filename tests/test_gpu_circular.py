@@ -57,15 +57,20 @@ def test_circular_sisi(cuda_ready, fx, ik):
     assert (r["iters"] > 0).all()
 
 
-@pytest.mark.parametrize("nc,precision,tol", [(2, "fp64", 1e-9), (3, "fp64", 1e-9), (3, "tc", 1e-9),
-                                              (2, "df64", 1e-6)])
-def test_circular_diamond_gamma(cuda_ready, nc, precision, tol):
+@pytest.mark.parametrize("nc,cells,precision,tol", [(2, (2, 2), "fp64", 1e-9), (3, (3, 3), "fp64", 1e-9),
+                                                    (3, (3, 3), "tc", 1e-9), (2, (2, 2), "df64", 1e-6),
+                                                    (3, (3, 1), "fp64", 1e-9)])
+def test_circular_diamond_gamma(cuda_ready, nc, cells, precision, tol):
+    """Small blocks of 24 (resident decimation, one CTA a block; batched
+    double-float engine for df64) and, with 3 x 1 cells, of 72 (batched
+    small-block engine)."""
     b, E, p, aux = S.diamond_phonon(nc=nc, L=6, nk_side=1, ne=12)
     bq = {k: v[0] for k, v in b.items()}
     E = E[1::2]
-    r = transport_tdb(E, bq, want_transr=False, circular=(nc, nc, [TWO_PI] * 4), precision=precision, **p)
+    ny, nx = cells
+    r = transport_tdb(E, bq, want_transr=False, circular=(ny, nx, [TWO_PI] * 4), precision=precision, **p)
     assert (r["status"] == 0).all()
-    To = C.transport_circular(E, bq, p["eta"], p["eta0"], p["convergence"], p["dev_factor"], nc, nc,
+    To = C.transport_circular(E, bq, p["eta"], p["eta0"], p["convergence"], p["dev_factor"], ny, nx,
                               [TWO_PI] * 4)
     assert To.max() > 1.0
     assert _rel(r["transl"], To).max() < tol, _rel(r["transl"], To).max()
