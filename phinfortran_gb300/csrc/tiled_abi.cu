@@ -300,10 +300,27 @@ __global__ void k_circ_fwd(const cx<T>* h00, const cx<T>* v, int m, int ny, int 
 // g_b = P1 diag_i(P2 diag_j(gs[b K + i nx + j]) P2^H) P1^H:
 //   g((a nx + u) s + r, (a' nx + u') s + c)
 //     = 1/K sum_i w_y^{i (a - a')} sum_j w_x^{j (u - u')} gs[b K + i nx + j](r, c)
-// Grid (ceil(m*m/256), batch).
+// The phases w_y^{i d} (d = a - a' in (-ny, ny)) and w_x^{j d} are tabulated
+// in shared memory first: ny (2 ny - 1) + nx (2 nx - 1) entries, at most
+// kCircTab (the entry refuses larger cell counts).  Grid (ceil(m*m/256), batch).
+constexpr int kCircTab = 2048;  // phase-table entries (complex double, 32 KB) of k_circ_back
 template <typename T>
 __global__ void k_circ_back(cx<T>* out, long long so, int ld, const cx<T>* gs, int m, int ny, int nx, double gry,
                             double grx) {
+  __shared__ double2 tab[kCircTab];
+  const int ty = ny * (2 * ny - 1), tx = nx * (2 * nx - 1);
+  for (int t = threadIdx.x; t < ty + tx; t += blockDim.x) {
+    double sn, cs;
+    if (t < ty) {
+      const int i = t / (2 * ny - 1), d = t % (2 * ny - 1) - (ny - 1);
+      sincos(gry * (double)(i * d) / (double)ny, &sn, &cs);
+    } else {
+      const int u = t - ty, j = u / (2 * nx - 1), d = u % (2 * nx - 1) - (nx - 1);
+      sincos(grx * (double)(j * d) / (double)nx, &sn, &cs);
+    }
+    tab[t] = make_double2(cs, sn);
+  }
+  __syncthreads();
   const int b = blockIdx.y;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m * m) return;
@@ -312,20 +329,20 @@ __global__ void k_circ_back(cx<T>* out, long long so, int ld, const cx<T>* gs, i
   const int a = R / (nx * s), u = (R / s) % nx, r = R % s;
   const int a2 = Cc / (nx * s), u2 = (Cc / s) % nx, c = Cc % s;
   const cx<T>* g = gs + (size_t)b * K * s * s + r + (size_t)c * s;
+  const double2* wy = tab + (a - a2 + ny - 1);
+  const double2* wx = tab + ty + (u - u2 + nx - 1);
   double xr = 0.0, xi = 0.0;
   for (int i = 0; i < ny; ++i) {
     double yr = 0.0, yi = 0.0;
     for (int j = 0; j < nx; ++j) {
       const cx<T> v = g[(size_t)(i * nx + j) * s * s];
-      double sn, cs;
-      sincos(grx * (double)(j * (u - u2)) / (double)nx, &sn, &cs);
-      yr += pf::to_d(v.x) * cs - pf::to_d(v.y) * sn;
-      yi += pf::to_d(v.x) * sn + pf::to_d(v.y) * cs;
+      const double2 w = wx[j * (2 * nx - 1)];
+      yr += pf::to_d(v.x) * w.x - pf::to_d(v.y) * w.y;
+      yi += pf::to_d(v.x) * w.y + pf::to_d(v.y) * w.x;
     }
-    double sn, cs;
-    sincos(gry * (double)(i * (a - a2)) / (double)ny, &sn, &cs);
-    xr += yr * cs - yi * sn;
-    xi += yr * sn + yi * cs;
+    const double2 w = wy[i * (2 * ny - 1)];
+    xr += yr * w.x - yi * w.y;
+    xi += yr * w.y + yi * w.x;
   }
   out[(size_t)b * so + R + (size_t)Cc * ld] = pf::mk<T>(T(xr / K), T(xi / K));
 }
@@ -980,6 +997,8 @@ size_t tiled_bytes(int n, int nl, int nr, int L, int nq, int npts, int arith, in
 const char* circ_dims_error(int nl, int nr, int ny, int nx) {
   if (ny < 1 || nx < 1) return "pf_tiled_circ: n_bloch_y and n_bloch_x must be positive";
   if ((long long)ny * nx > 256) return "pf_tiled_circ: at most 256 Bloch cells";
+  if ((long long)ny * (2 * ny - 1) + (long long)nx * (2 * nx - 1) > kCircTab)
+    return "pf_tiled_circ: n_bloch_y, n_bloch_x too large for the phase table";
   if (nl != nr) return "pf_tiled_circ: block-circulant leads need nl == nr";
   if (nl <= 0 || nl % (ny * nx)) return "pf_tiled_circ: nl must be a multiple of n_bloch_y * n_bloch_x";
   return nullptr;

@@ -143,6 +143,7 @@ def test_tiled_circular_validation_without_gpu(built_lib):
     assert ws(96, 96, 96, 10, 1, 64, 0, 5, 2) == 0
     assert ws(96, 96, 48, 10, 1, 64, 0, 2, 2) == 0
     assert ws(96, 96, 96, 10, 1, 64, 0, 0, 2) == 0
+    assert ws(66, 66, 66, 10, 1, 64, 0, 33, 1) == 0     # phase table of the back transform
     gr = (C.c_double * 4)(*([6.283185307179586] * 4))
     args = [96, 96, 96, 10, 1] + [None] * 8 + [1, None, None, None, 0.0, 1e-5, 10.0, 1e-14, 100, 0]
     rc = lib.pf_transport_tdb_tiled_circ_dev(*args, 5, 2, gr, None, None, None, None, 0, None)
