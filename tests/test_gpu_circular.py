@@ -76,6 +76,24 @@ def test_circular_diamond_gamma(cuda_ready, nc, cells, precision, tol):
     assert _rel(r["transl"], To).max() < tol, _rel(r["transl"], To).max()
 
 
+def test_circular_sisi_two_q(cuda_ready, fx):
+    """Two k block sets interleaved in one call (qidx): every q batch is
+    transformed with its own lead matrices."""
+    p = sisi_params(fx)
+    bs = [{k: np.asarray(v) for k, v in sisi_blocks(fx, ik).items()} for ik in (3, 40)]
+    st = {k: np.stack([bs[0][k], bs[1][k]]) for k in bs[0]}
+    E1 = np.asarray(fx["E"][2:60:7], dtype=np.float64)
+    E = np.repeat(E1, 2)
+    q = np.tile(np.array([0, 1], dtype=np.int32), E1.size)
+    gr = _sisi_gr(fx)
+    r = transport_tdb(E, st, qidx=q, want_transr=False, circular=(2, 2, gr), **p)
+    assert (r["status"] == 0).all()
+    for qq in (0, 1):
+        sel = q == qq
+        To = C.transport_circular(E[sel], bs[qq], p["eta"], p["eta0"], p["convergence"], p["dev_factor"], 2, 2, gr)
+        assert _rel(r["transl"][sel], To).max() < 1e-9
+
+
 def test_circular_reads_first_block_rows(cuda_ready, fx):
     """Rows of H_L below the first block row perturbed: the direct
     decimation changes, circular_g does not (it transforms the first block
