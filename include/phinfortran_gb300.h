@@ -438,6 +438,39 @@ int pf_transport_tdb_modes_ex_dev(int n, int nl, int nr, int L, int nq,
                                   void* stream);
 
 /*
+ * pf_transport_tdb_modes_ex_dev plus the whole mode-to-mode matrices of
+ * vel_mat_tdb, what write_md2md prints with verbosity = 1
+ * (negf/velocity_mat.f90:3132-3145, negf/write_data.f90:177-241):
+ * md2md[npts][4][mm][mm] (mm = max(nl, nr); matrices tlr, trl, rrr, rll;
+ * column c, row r at [p][matrix][c][r]) = |M_rc|^2, rows the outgoing modes
+ * of mode_kz's problem (ret-L, ret-R, ret-R, ret-L), columns the incoming
+ * (adv-R, adv-L, adv-R, adv-L), zero outside the lead sizes and at points
+ * with zero_flag.  md2md needs the per-mode outputs; null md2md is
+ * pf_transport_tdb_modes_ex_dev.
+ */
+int pf_transport_tdb_modes_md2md_dev(int n, int nl, int nr, int L, int nq,
+                                     const double* HL, const double* HLv,
+                                     const double* HR, const double* HRv,
+                                     const double* Hd, const double* Hdv,
+                                     const double* Hld, const double* Hrd,
+                                     int npts, const double* E,
+                                     const int* qidx, const int* zero_flag,
+                                     double eta, double eta0,
+                                     double dev_factor, double convergence,
+                                     int max_iter, double lambda_eta,
+                                     double a_z_l, double a_z_r, int nshift,
+                                     int stride_l, int nrep_l,
+                                     const double* phase_l, int stride_r,
+                                     int nrep_r, const double* phase_r, int flags,
+                                     double* transl, double* transr,
+                                     double* mode_sums, int* status,
+                                     int* nprop, double* mode_kz,
+                                     int* mode_bz, double* col_sums,
+                                     double* md2md,
+                                     void* work, size_t work_bytes,
+                                     void* stream);
+
+/*
  * The FP64 transport of one batch (T_L, T_R, status) plus the Green's
  * functions that the reference's vel_mat_tdb receives from
  * surface_green_tdb_mpi (negf/surface.f90:344-383: the four decimations)

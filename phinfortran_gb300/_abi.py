@@ -111,6 +111,17 @@ SIGNATURES = {
                                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                 C.c_void_p, C.c_void_p, C.c_void_p,
                                                 C.c_void_p, C.c_size_t, C.c_void_p]),
+    "pf_transport_tdb_modes_md2md_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                   C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                   C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                                   C.c_double, C.c_double, C.c_double,
+                                                   C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int,
+                                                   C.c_void_p, C.c_int,
+                                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                   C.c_void_p, C.c_size_t, C.c_void_p]),
     "pf_transport_tdb_modes_permode_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

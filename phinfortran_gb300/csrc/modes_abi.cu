@@ -118,6 +118,7 @@ struct ModeOut {
   int* mode_bz;      // [npts][4 problems][mm] unfolding label (0: not propagating)
   double* col_sums;  // [npts][4 matrices][mm columns][nshift] sum of |M_rc|^2 over the rows of each label
   int mm;            // max(nl, nr)
+  double* md2md;     // [npts][4 matrices][mm columns][mm rows] |M_rc|^2 (nullable)
 };
 
 // reference value of pi (negf/util.f90:5)
@@ -453,6 +454,16 @@ __global__ void __launch_bounds__(kTaskThreads)
   // mat 0 tlr, 1 trl, 2 rrr, 3 rll; columns without a label stay zero
   const int nsh = geo.nshift;
   auto col_out = [&](int mat, int rows, int cols, const int* bzr, const int* bzc) {
+    if (out.md2md) {
+      // the whole mode-to-mode matrix |M_rc|^2 (write_md2md, negf/write_data.f90:177-241)
+      double* o = out.md2md + ((size_t)p * 4 + mat) * out.mm * out.mm;
+      for (int u = threadIdx.x; u < rows * cols; u += blockDim.x) {
+        const int r = u % rows, c = u / rows;
+        const C e = t.s[0][r + c * ld];
+        o[r + (size_t)c * out.mm] = e.x * e.x + e.y * e.y;
+      }
+      __syncthreads();
+    }
     if (!out.col_sums) return;
     double* o = out.col_sums + ((size_t)p * 4 + mat) * out.mm * nsh;
     for (int u = threadIdx.x; u < cols * nsh; u += blockDim.x) {
@@ -471,6 +482,11 @@ __global__ void __launch_bounds__(kTaskThreads)
   if (out.col_sums) {
     double* o = out.col_sums + (size_t)p * 4 * out.mm * nsh;
     for (int u = threadIdx.x; u < 4 * out.mm * nsh; u += blockDim.x) o[u] = 0.0;
+    __syncthreads();
+  }
+  if (out.md2md) {
+    double* o = out.md2md + (size_t)p * 4 * out.mm * out.mm;
+    for (int u = threadIdx.x; u < 4 * out.mm * out.mm; u += blockDim.x) o[u] = 0.0;
     __syncthreads();
   }
   // prefactor of the t / r chains: 2 sqrt(E / (a_row a_col)) (phonons), 1 (electrons)
@@ -627,7 +643,25 @@ int pf_transport_tdb_modes_ex_dev(int n, int nl, int nr, int L, int nq, const do
                                   int flags, double* transl, double* transr, double* mode_sums, int* status,
                                   int* nprop, double* mode_kz, int* mode_bz, double* col_sums, void* work,
                                   size_t work_bytes, void* stream) {
+  return pf_transport_tdb_modes_md2md_dev(n, nl, nr, L, nq, HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd, npts, E, qidx,
+                                          zero_flag, eta, eta0, dev_factor, convergence, max_iter, lambda_eta,
+                                          a_z_l, a_z_r, nshift, stride_l, nrep_l, phase_l, stride_r, nrep_r,
+                                          phase_r, flags, transl, transr, mode_sums, status, nprop, mode_kz,
+                                          mode_bz, col_sums, nullptr, work, work_bytes, stream);
+}
+
+int pf_transport_tdb_modes_md2md_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
+                                     const double* HR, const double* HRv, const double* Hd, const double* Hdv,
+                                     const double* Hld, const double* Hrd, int npts, const double* E,
+                                     const int* qidx, const int* zero_flag, double eta, double eta0,
+                                     double dev_factor, double convergence, int max_iter, double lambda_eta,
+                                     double a_z_l, double a_z_r, int nshift, int stride_l, int nrep_l,
+                                     const double* phase_l, int stride_r, int nrep_r, const double* phase_r,
+                                     int flags, double* transl, double* transr, double* mode_sums, int* status,
+                                     int* nprop, double* mode_kz, int* mode_bz, double* col_sums,
+                                     double* md2md, void* work, size_t work_bytes, void* stream) {
   if (flags & ~PF_MODES_ELECTRON) return set_err(PF_ERR_ARG, "pf_modes: unknown flags");
+  if (md2md && !mode_kz) return set_err(PF_ERR_ARG, "pf_modes: md2md needs the per-mode outputs");
   if ((mode_kz != nullptr) != (mode_bz != nullptr) || (mode_kz != nullptr) != (col_sums != nullptr))
     return set_err(PF_ERR_ARG, "pf_modes: mode_kz, mode_bz and col_sums are all given or all null");
   if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0)
@@ -696,7 +730,7 @@ int pf_transport_tdb_modes_ex_dev(int n, int nl, int nr, int L, int nq, const do
   geo.nrep_r = nrep_r;
   geo.phase_l = reinterpret_cast<const cx<double>*>(phase_l);
   geo.phase_r = reinterpret_cast<const cx<double>*>(phase_r);
-  ModeOut out{transl, transr, mode_sums, status, nprop, mode_kz, mode_bz, col_sums, nl > nr ? nl : nr};
+  ModeOut out{transl, transr, mode_sums, status, nprop, mode_kz, mode_bz, col_sums, nl > nr ? nl : nr, md2md};
   for (int p0 = 0; p0 < npts; p0 += chunk) {
     const int cnt = (npts - p0) < chunk ? (npts - p0) : chunk;
     MD_CUDA(cudaMemsetAsync(queue, 0, sizeof(int), st));

@@ -138,7 +138,7 @@ class LeadGeometry:
 
 def transport_tdb_modes(E, blocks, geometry, ksc, *, eta, eta0, convergence, lambda_eta, a_z_l, a_z_r,
                         dev_factor=10.0, qidx=None, zero_flag=None, max_iter=1000, check=True, per_mode=False,
-                        electron=False):
+                        electron=False, md2md=False):
     """Transmission and its mode-resolved split for a batch of points.
 
     ``blocks``: one q (dict) or a TdbBlocks stack; ``ksc``: (nq, 3)
@@ -149,7 +149,9 @@ def transport_tdb_modes(E, blocks, geometry, ksc, *, eta, eta0, convergence, lam
     (problems adv-L, ret-L, ret-R, adv-R; matrices tlr, trl, rrr, rll).
     ``electron`` selects the tight-binding normalisation (velocity matrices
     and t / r without the phonon a_z / (2 sqrt(E)) factors; energies may be
-    negative).
+    negative).  ``md2md`` (implies ``per_mode``) adds the whole mode-to-mode
+    matrices |M_rc|^2 as md2md (npts, 4, mm rows, mm columns)
+    (pf_transport_tdb_modes_md2md_dev), what write_md2md prints.
     """
     import torch
     lib = _abi.load()
@@ -185,13 +187,15 @@ def transport_tdb_modes(E, blocks, geometry, ksc, *, eta, eta0, convergence, lam
     outs = (tl.data_ptr(), tr.data_ptr(), sums.data_ptr(), st.data_ptr(), npr.data_ptr())
     tail = (work.data_ptr(), ws, C.c_void_p(torch.cuda.current_stream().cuda_stream))
     flags = 1 if electron else 0   # PF_MODES_ELECTRON
+    per_mode = per_mode or md2md
     if per_mode:
         mm = max(nl, nr)
         kz = torch.zeros((max(npts, 1), 4, mm), dtype=torch.float64, device="cuda")
         bz = torch.zeros((max(npts, 1), 4, mm), dtype=torch.int32, device="cuda")
         cs = torch.zeros((max(npts, 1), 4, mm, geometry.nshift), dtype=torch.float64, device="cuda")
-        rc = lib.pf_transport_tdb_modes_ex_dev(*head, flags, *outs, kz.data_ptr(), bz.data_ptr(), cs.data_ptr(),
-                                               *tail)
+        m2 = torch.zeros((max(npts, 1), 4, mm, mm), dtype=torch.float64, device="cuda") if md2md else None
+        rc = lib.pf_transport_tdb_modes_md2md_dev(*head, flags, *outs, kz.data_ptr(), bz.data_ptr(),
+                                                  cs.data_ptr(), p(m2), *tail)
     else:
         rc = lib.pf_transport_tdb_modes_ex_dev(*head, flags, *outs, None, None, None, *tail)
     if rc != 0:
@@ -208,6 +212,9 @@ def transport_tdb_modes(E, blocks, geometry, ksc, *, eta, eta0, convergence, lam
     if per_mode:
         out.update(mode_kz=kz.cpu().numpy()[:npts], mode_bz=bz.cpu().numpy()[:npts],
                    col_sums=cs.cpu().numpy()[:npts], nl=nl, nr=nr)
+        if md2md:
+            # device layout [p][matrix][column][row] -> (npts, 4, rows, columns)
+            out["md2md"] = np.ascontiguousarray(np.swapaxes(m2.cpu().numpy()[:npts], -1, -2))
     return out
 
 
@@ -278,6 +285,92 @@ MODE_FILES = ("left", "right", "tlr", "trl", "mdl", "mdr")
 
 def _clamp(x):
     return 1.0e-60 if 0.0 < x < 1.0e-60 else x
+
+
+def _pc_columns(res, labk, q_of, E, pcs, kinds):
+    """Primitive-cell k and velocity (npts, modes, 6) of the propagating
+    modes of each problem kind, one unfolding batch per kind (zero without
+    a primitive cell)."""
+    size = {"adv_l": res["nl"], "ret_l": res["nl"], "ret_r": res["nr"], "adv_r": res["nr"]}
+    npts = E.size
+    pcol = {}
+    for kind in kinds:
+        side = 0 if kind.endswith("_l") else 1
+        ki = KINDS.index(kind)
+        cols = np.zeros((npts, size[kind], 6))
+        if pcs[side] is not None:
+            kz, bz = res["mode_kz"][:, ki, :size[kind]], res["mode_bz"][:, ki, :size[kind]]
+            pp, ii = np.nonzero((kz < 99.9) & (bz > 0))
+            if pp.size:
+                lk = np.array([labk[int(q_of[a])][bz[a, i] - 1] for a, i in zip(pp, ii)])
+                lk[:, 2] = kz[pp, ii]
+                kp, vp = pcs[side].unfold(E[pp], lk)
+                cols[pp, ii, :3], cols[pp, ii, 3:] = kp, vp
+        pcol[kind] = cols
+    return pcol
+
+
+def _mode_k(res, p, kind, lk):
+    """(modes, 3) k of every mode of one problem: the label's in-plane k
+    with the mode's k_z, 100 for the modes that do not propagate."""
+    size = res["nl"] if kind.endswith("_l") else res["nr"]
+    ki = KINDS.index(kind)
+    kz, bz = res["mode_kz"][p, ki], res["mode_bz"][p, ki]
+    k = np.full((size, 3), 100.0)
+    for i in range(size):
+        if kz[i] < 99.9 and bz[i] > 0:
+            k[i] = lk[bz[i] - 1]
+            k[i, 2] = kz[i]
+    return k
+
+
+# write_md2md calls (velocity_mat.f90:3132-3145): file -> (matrix, row problem k_f, column problem k_b)
+MD2MD_FILES = {"tlr": ("tlr", "ret_l", "adv_r"), "trl": ("trl", "ret_r", "adv_l"),
+               "rrr": ("rrr", "ret_r", "adv_r"), "rll": ("rll", "ret_l", "adv_l")}
+
+
+def md2md_rows(res, geometry, ksc, E, qidx=None, pc=None):
+    """Rows of the mode-to-mode files of write_md2md
+    (negf/write_data.f90:177-241) for every point of a run with
+    ``md2md=True``: {direction: [(q, rows)] per point}, a row (count1,
+    count2, omega, k_f(3), k_b(3), kpc_f(3), kpc_b(3), v_f(3), v_b(3), ts,
+    tns, i, j) for every pair of propagating modes, j over the column
+    problem (outer loop) and i over the row problem, count2 counting the
+    columns and count1 every pair; |M_ij|^2 goes to ts when the in-plane k
+    of the two modes agree within 1e-5 (squared), else to tns.  Mode order
+    as in ``mode_rows``."""
+    ksc = np.atleast_2d(np.asarray(ksc, dtype=np.float64))
+    E = np.asarray(E, dtype=np.float64)
+    npts = E.size
+    q_of = np.zeros(npts, dtype=np.int64) if qidx is None else np.asarray(qidx, dtype=np.int64)
+    labk = [geometry.label_k(k) for k in ksc]
+    pcs = (pc, pc) if pc is None or not isinstance(pc, (tuple, list)) else tuple(pc)
+    pcol = _pc_columns(res, labk, q_of, E, pcs, KINDS)
+    out = {d: [] for d in MD2MD_FILES}
+    for p in range(npts):
+        q = int(q_of[p])
+        lk = labk[q]
+        w = float(np.sqrt(E[p]))
+        for d, (mat, kf_kind, kb_kind) in MD2MD_FILES.items():
+            M = res["md2md"][p, MATRICES.index(mat)]
+            kf, kb = _mode_k(res, p, kf_kind, lk), _mode_k(res, p, kb_kind, lk)
+            pf_, pb = pcol[kf_kind][p], pcol[kb_kind][p]
+            rows, c1, c2 = [], 0, 0
+            for j in range(kb.shape[0]):
+                if kb[j, 2] >= 99.9:
+                    continue
+                c2 += 1
+                for i in range(kf.shape[0]):
+                    if kf[i, 2] >= 99.9:
+                        continue
+                    c1 += 1
+                    dk = kf[i, :2] - kb[j, :2]
+                    v = float(M[i, j])
+                    ts, tns = (v, 0.0) if float(dk @ dk) < 1.0e-5 else (0.0, v)
+                    rows.append((c1, c2, w, *kf[i], *kb[j], *pf_[i, :3], *pb[j, :3], *pf_[i, 3:], *pb[j, 3:],
+                                 ts, tns, i + 1, j + 1))
+            out[d].append((q, rows))
+    return out
 
 
 def mode_rows(res, geometry, ksc, E, qidx=None, pc=None):

@@ -114,3 +114,31 @@ def write_mode_files(output_dir, rows, k_index=None):
         finally:
             for f in files.values():
                 f.close()
+
+
+def md2md_line(row):
+    """One row of a mode-to-mode file: format 1000 of write_md2md
+    (negf/write_data.f90:239), (2I5, 21E20.10, 2I5)."""
+    c1, c2, *vals = row
+    i, j = vals[-2:]
+    return (f"{int(c1):5d}{int(c2):5d}" + "".join(fortran_e(v, 20, 10) for v in vals[:-2]) +
+            f"{int(i):5d}{int(j):5d}\n")
+
+
+def write_md2md_files(output_dir, rows, k_index=None):
+    """Append the mode-to-mode files ``{direction}_md2md_{k:06d}.dat``
+    (write_md2md, negf/write_data.f90:177-241, written by vel_mat_tdb with
+    verbosity = 1, velocity_mat.f90:3132-3145) for the rows of
+    ``modes.md2md_rows``; ``k_index`` maps q to the 1-based k number."""
+    os.makedirs(output_dir, exist_ok=True)
+    for direction, per_point in rows.items():
+        files = {}
+        try:
+            for q, rr in per_point:
+                k = (k_index[q] if k_index is not None else q + 1)
+                if k not in files:
+                    files[k] = open(os.path.join(output_dir, f"{direction}_md2md_{int(k):06d}.dat"), "a")
+                files[k].writelines(md2md_line(r) for r in rr)
+        finally:
+            for f in files.values():
+                f.close()

@@ -7,6 +7,7 @@
     python -m phinfortran_gb300.run sc       --layers 40 --energies 64 --mode grad --arith df64
     python -m phinfortran_gb300.run sisi     --kpoints 1 --energies 16 --mode modes
     python -m phinfortran_gb300.run sisi     --kpoints 49 --energies 61 --mode modes --out out/
+    python -m phinfortran_gb300.run sisi     --kpoints 3 --energies 61 --mode modes --out out/ --md2md
 
 Modes: ``transport`` (T per point), ``modes`` (T plus the s/ns sums of the
 mode-resolved transmission; si-si fixture only), ``grad`` (adjoint: T and
@@ -75,6 +76,8 @@ def main():
                          "(circular_flag = 1, nc x nc Bloch cells)")
     ap.add_argument("--out", default="",
                     help="sisi: write the reference's ten output tables and the per-k mode files into this directory")
+    ap.add_argument("--md2md", action="store_true",
+                    help="sisi with --out: also the mode-to-mode files (the reference's verbosity = 1)")
     a = ap.parse_args()
     import torch
     out = dict(workload=a.workload, mode=a.mode)
@@ -105,7 +108,7 @@ def main():
         t0 = time.perf_counter()
         r = transport_tdb_modes(E, blocks, geo, f["kgrid"][ks], qidx=q, zero_flag=zf, lambda_eta=5e-3,
                                 a_z_l=f["cell"][2, 2], a_z_r=f["cell"][2, 2], check=False,
-                                per_mode=bool(a.out), **p)
+                                per_mode=bool(a.out), md2md=bool(a.out) and a.md2md, **p)
         torch.cuda.synchronize()
         out.update(points=int(E.size), seconds=time.perf_counter() - t0, transl=r["transl"].tolist(),
                    transl_s=r["transl_s"].tolist(), status=int(np.bitwise_or.reduce(r["status"])))
@@ -122,6 +125,11 @@ def main():
                                f["mass_no"], 2 * np.pi * np.linalg.inv(f["cell"]).T, max(nb))
             write_mode_files(a.out, mode_rows(r, geo, f["kgrid"][ks], E, qidx=q, pc=pc),
                              k_index={i: k + 1 for i, k in enumerate(ks)})
+            if a.md2md:
+                from .modes import md2md_rows
+                from .output import write_md2md_files
+                write_md2md_files(a.out, md2md_rows(r, geo, f["kgrid"][ks], E, qidx=q, pc=pc),
+                                  k_index={i: k + 1 for i, k in enumerate(ks)})
             out["written"] = a.out
         print(json.dumps(out))
         return

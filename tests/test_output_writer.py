@@ -59,3 +59,15 @@ def test_clamp_and_row_endings(tmp_path):
     assert tot[1].endswith(W.fortran_e(0.0))
     s = open(tmp_path / "transl_s.dat").read().splitlines()
     assert s[0].endswith(" ") and not tot[0].endswith(" ")
+
+
+def test_md2md_line_format():
+    """write_md2md's format 1000 (negf/write_data.f90:239): 2I5, 21E20.10, 2I5."""
+    from phinfortran_gb300.output import md2md_line
+    row = (3, 1, 2.5, *([0.125] * 18), 0.25, 0.0, 2, 1)
+    s = md2md_line(row)
+    assert s.endswith("\n") and len(s) == 5 * 2 + 20 * 21 + 5 * 2 + 1
+    assert s.startswith("    3    1") and s.rstrip("\n").endswith("    2    1")
+    vals = s[10:10 + 20 * 21]
+    assert vals[:20] == "    0.2500000000E+01"
+    assert vals[20 * 19:20 * 20] == "    0.2500000000E+00" and vals[20 * 20:] == "    0.0000000000E+00"
