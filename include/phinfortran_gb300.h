@@ -594,6 +594,31 @@ int pf_transport_tdb_tiled_circ_dev(int n, int nl, int nr, int L, int nq,
                                     double* transl, int* status, int* iters,
                                     void* work, size_t work_bytes, void* stream);
 
+/* The large-block entry with every option: the block-circulant leads of
+ * pf_transport_tdb_tiled_circ_dev (n_bloch_y = n_bloch_x = 1: off, gr may
+ * be NULL, any nl, nr) and, when transr is not NULL, T_R as well: the
+ * right-to-left sweep of get_G_full_tdb (negf/lesser.f90:694-784) with the
+ * left closure G_{0,0} = inv(z - H_L - Sigma_L - H_ld g_1 H_ld^H) and
+ * T_R = Re Tr[G_{N+1,0} Gamma_L G_{N+1,0}^H Gamma_R] (:794-800), a second
+ * sweep's cost.  work: pf_transport_tdb_tiled_ex_workspace_size bytes. */
+size_t pf_transport_tdb_tiled_ex_workspace_size(int n, int nl, int nr, int L, int nq,
+                                                int npts, int arith, int n_bloch_y,
+                                                int n_bloch_x);
+
+int pf_transport_tdb_tiled_ex_dev(int n, int nl, int nr, int L, int nq,
+                                  const double* HL, const double* HLv,
+                                  const double* HR, const double* HRv,
+                                  const double* Hd, const double* Hdv,
+                                  const double* Hld, const double* Hrd,
+                                  int npts, const double* E, const int* qidx,
+                                  const int* zero_flag,
+                                  double eta, double eta0, double dev_factor,
+                                  double convergence, int max_iter, int arith,
+                                  int n_bloch_y, int n_bloch_x, const double* gr,
+                                  double* transl, double* transr, int* status,
+                                  int* iters, void* work, size_t work_bytes,
+                                  void* stream);
+
 /* Message for the last error of the large-block entry points. */
 const char* pf_tiled_last_error(void);
 

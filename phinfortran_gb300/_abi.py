@@ -151,6 +151,15 @@ SIGNATURES = {
                                                   C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
                                                   C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_size_t, C.c_void_p]),
+    "pf_transport_tdb_tiled_ex_workspace_size": (C.c_size_t, [C.c_int] * 9),
+    "pf_transport_tdb_tiled_ex_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                                C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_size_t, C.c_void_p]),
     "pf_tc_last_error": (C.c_char_p, []),
     "pf_tc_zgemm_workspace_size": (C.c_size_t, [C.c_int] * 6),
     "pf_tc_zgemm_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,

@@ -752,7 +752,8 @@ struct Engine {
 
   // One batch of points sharing block set q: leads, sweep, Caroli.
   int run(const pf::System<T>& sys, int q, const double* E, int cnt, double eta, double eta0, double devf,
-          double conv, int max_iter, bool mirror, const int* zero_flag, double* transl, int* status, int* iters) {
+          double conv, int max_iter, bool mirror, const int* zero_flag, double* transl, int* status, int* iters,
+          double* transr = nullptr) {
     const int n = L.n, nl = L.nl, nr = L.nr, Ld = sys.L, ld = L.m;
     const long long sm = (long long)L.mat;
     const cx<T> one = hc<T>(1.0), zero = hc<T>(0.0), mone = hc<T>(-1.0);
@@ -833,6 +834,38 @@ struct Engine {
     k_trace<T><<<cnt, 256, 0, s>>>(U, g, sm, nl, nr, ld, w.idx, zero_flag, w.st, w.itl, w.itr, transl, status,
                                    iters);
     TL_CUDA(cudaGetLastError());
+    if (!transr) return PF_SUCCESS;
+    // ---- right-to-left sweep (lesser.f90:694-784), T_R (:794-800)
+    // layer N: T1 = gr Hrd (nr x n); g = inv(zD - Hd_N - Hrd^H T1); GNo = T1 g
+    TL_CUDA(gemm(nr, n, nr, gr, ld, sm, false, Hrd, nr, 0, false, T1, ld, sm, one, zero, nullptr));
+    TL_CUDA(gemm(n, n, nr, Hrd, nr, 0, true, T1, ld, sm, false, g, ld, sm, mone, zero, nullptr, w.zd,
+                 Hd + (size_t)(Ld - 1) * n * n, n, 0));
+    if ((rc = inverse(g, n, nullptr))) return rc;
+    TL_CUDA(gemm(nr, n, n, T1, ld, sm, false, g, ld, sm, false, G0N, ld, sm, one, zero, nullptr));
+    for (int i = Ld - 1; i >= 1; --i) {
+      // V = Hdv_i^H couples layer i + 1 to layer i
+      const cx<T>* V = Hdv + (size_t)(i - 1) * n * n;
+      TL_CUDA(gemm(n, n, n, g, ld, sm, false, V, n, 0, true, T1, ld, sm, one, zero, nullptr));
+      TL_CUDA(gemm(n, n, n, V, n, 0, false, T1, ld, sm, false, A, ld, sm, mone, zero, nullptr, w.zd,
+                   Hd + (size_t)(i - 1) * n * n, n, 0));
+      if ((rc = inverse(A, n, nullptr))) return rc;
+      TL_CUDA(gemm(nr, n, n, G0N, ld, sm, false, V, n, 0, true, U, ld, sm, one, zero, nullptr));
+      TL_CUDA(gemm(nr, n, n, U, ld, sm, false, A, ld, sm, false, G0N, ld, sm, one, zero, nullptr));
+      std::swap(g, A);
+    }
+    // left closure: A = inv(zD - HL - sl - Hld g Hld^H); G_{N+1,0} = GNo Hld^H A
+    TL_CUDA(gemm(n, nl, n, g, ld, sm, false, Hld, nl, 0, true, T1, ld, sm, one, zero, nullptr));
+    TL_CUDA(gemm(nl, nl, n, Hld, nl, 0, false, T1, ld, sm, false, A, ld, sm, mone, zero, nullptr, w.zd, HL, nl, 0));
+    k_sub<T><<<eg(nl * nl), 256, 0, s>>>(A, sl, sm, nl, ld);
+    if ((rc = inverse(A, nl, nullptr))) return rc;
+    TL_CUDA(gemm(nr, nl, n, G0N, ld, sm, false, Hld, nl, 0, true, U, ld, sm, one, zero, nullptr));
+    TL_CUDA(gemm(nr, nl, nl, U, ld, sm, false, A, ld, sm, false, T1, ld, sm, one, zero, nullptr));  // G_D_RL
+    // Caroli: Re Tr[(G_D_RL gml)(G_D_RL^H gmr)]
+    TL_CUDA(gemm(nr, nl, nl, T1, ld, sm, false, gml, ld, sm, false, U, ld, sm, one, zero, nullptr));
+    TL_CUDA(gemm(nl, nr, nr, T1, ld, sm, true, gmr, ld, sm, false, g, ld, sm, one, zero, nullptr));
+    k_trace<T><<<cnt, 256, 0, s>>>(U, g, sm, nr, nl, ld, w.idx, zero_flag, w.st, w.itl, w.itr, transr, status,
+                                   nullptr);
+    TL_CUDA(cudaGetLastError());
     return PF_SUCCESS;
   }
 };
@@ -850,7 +883,7 @@ template <typename T>
 int drive(int n, int nl, int nr, int L, int nq, const double* const blk[8], int npts, const double* E,
           const int* qidx, const int* zero_flag, double eta, double eta0, double dev_factor, double convergence,
           int max_iter, double* transl, int* status, int* iters, char* base, size_t work_bytes, cudaStream_t st,
-          int arith, const Circ* circ) {
+          int arith, const Circ* circ, double* transr) {
   Engine<T> e;
   const bool tc = arith == PF_ARITH_TC;
   const int K = circ ? circ->K() : 1;
@@ -955,7 +988,7 @@ int drive(int n, int nl, int nr, int L, int nq, const double* const blk[8], int 
       }
       e.B = cnt;
       const int rc = e.run(sys, 0, E, cnt, eta, eta0, dev_factor, convergence, max_iter, mirror, zero_flag, transl,
-                           status, iters);
+                           status, iters, transr);
       if (rc) return rc;
     }
     i0 = i1;
@@ -1006,8 +1039,8 @@ const char* circ_dims_error(int nl, int nr, int ny, int nx) {
 
 int tiled_entry(int n, int nl, int nr, int L, int nq, const double* const blk[8], int npts, const double* E,
                 const int* qidx, const int* zero_flag, double eta, double eta0, double dev_factor, double convergence,
-                int max_iter, int arith, const Circ* circ, double* transl, int* status, int* iters, void* work,
-                size_t work_bytes, void* stream) {
+                int max_iter, int arith, const Circ* circ, double* transl, double* transr, int* status, int* iters,
+                void* work, size_t work_bytes, void* stream) {
   if (n <= 0 || nl <= 0 || nr <= 0 || L <= 0 || nq <= 0 || npts < 0)
     return set_err(PF_ERR_ARG, "pf_tiled: dimensions must be positive");
   if (n > PF_NMAX_TILED || nl > PF_NMAX_TILED || nr > PF_NMAX_TILED)
@@ -1023,9 +1056,9 @@ int tiled_entry(int n, int nl, int nr, int L, int nq, const double* const blk[8]
   char* base = reinterpret_cast<char*>(work);
   if (arith != PF_ARITH_DF64)
     return drive<double>(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence,
-                         max_iter, transl, status, iters, base, work_bytes, st, arith, circ);
+                         max_iter, transl, status, iters, base, work_bytes, st, arith, circ, transr);
   return drive<pf::df64>(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence,
-                         max_iter, transl, status, iters, base, work_bytes, st, arith, circ);
+                         max_iter, transl, status, iters, base, work_bytes, st, arith, circ, transr);
 }
 
 }  // namespace
@@ -1066,7 +1099,7 @@ int pf_transport_tdb_tiled_dev(int n, int nl, int nr, int L, int nq, const doubl
                                size_t work_bytes, void* stream) {
   const double* blk[8] = {HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd};
   return tiled_entry(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence, max_iter,
-                     arith, nullptr, transl, status, iters, work, work_bytes, stream);
+                     arith, nullptr, transl, nullptr, status, iters, work, work_bytes, stream);
 }
 
 size_t pf_transport_tdb_tiled_circ_workspace_size(int n, int nl, int nr, int L, int nq, int npts, int arith,
@@ -1084,18 +1117,44 @@ int pf_transport_tdb_tiled_circ_dev(int n, int nl, int nr, int L, int nq, const 
                                     void* work, size_t work_bytes, void* stream) {
   if (const char* why = circ_dims_error(nl, nr, n_bloch_y, n_bloch_x)) return set_err(PF_ERR_ARG, why);
   if (!gr) return set_err(PF_ERR_ARG, "pf_tiled_circ: null gr");
+  return pf_transport_tdb_tiled_ex_dev(n, nl, nr, L, nq, HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd, npts, E, qidx,
+                                       zero_flag, eta, eta0, dev_factor, convergence, max_iter, arith, n_bloch_y,
+                                       n_bloch_x, gr, transl, nullptr, status, iters, work, work_bytes, stream);
+}
+
+size_t pf_transport_tdb_tiled_ex_workspace_size(int n, int nl, int nr, int L, int nq, int npts, int arith,
+                                                int n_bloch_y, int n_bloch_x) {
+  if (n_bloch_y == 1 && n_bloch_x == 1) return tiled_bytes(n, nl, nr, L, nq, npts, arith, 1);
+  return pf_transport_tdb_tiled_circ_workspace_size(n, nl, nr, L, nq, npts, arith, n_bloch_y, n_bloch_x);
+}
+
+int pf_transport_tdb_tiled_ex_dev(int n, int nl, int nr, int L, int nq, const double* HL, const double* HLv,
+                                  const double* HR, const double* HRv, const double* Hd, const double* Hdv,
+                                  const double* Hld, const double* Hrd, int npts, const double* E, const int* qidx,
+                                  const int* zero_flag, double eta, double eta0, double dev_factor,
+                                  double convergence, int max_iter, int arith, int n_bloch_y, int n_bloch_x,
+                                  const double* gr, double* transl, double* transr, int* status, int* iters,
+                                  void* work, size_t work_bytes, void* stream) {
+  if (const char* why = circ_dims_error(nl, nr, n_bloch_y, n_bloch_x)) {
+    // one Bloch cell: no block-circulant option, any nl, nr
+    if (!(n_bloch_y == 1 && n_bloch_x == 1)) return set_err(PF_ERR_ARG, why);
+  }
+  const bool circ_on = n_bloch_y * n_bloch_x > 1;
+  if (circ_on && !gr) return set_err(PF_ERR_ARG, "pf_tiled_circ: null gr");
   Circ c;
-  c.ny = n_bloch_y;
-  c.nx = n_bloch_x;
-  c.gr_l[0] = gr[0];
-  c.gr_l[1] = gr[1];
-  c.gr_r[0] = gr[2];
-  c.gr_r[1] = gr[3];
-  for (int i = 0; i < 4; ++i)
-    if (!std::isfinite(gr[i])) return set_err(PF_ERR_ARG, "pf_tiled_circ: gr must be finite");
+  if (circ_on) {
+    c.ny = n_bloch_y;
+    c.nx = n_bloch_x;
+    c.gr_l[0] = gr[0];
+    c.gr_l[1] = gr[1];
+    c.gr_r[0] = gr[2];
+    c.gr_r[1] = gr[3];
+    for (int i = 0; i < 4; ++i)
+      if (!std::isfinite(gr[i])) return set_err(PF_ERR_ARG, "pf_tiled_circ: gr must be finite");
+  }
   const double* blk[8] = {HL, HLv, HR, HRv, Hd, Hdv, Hld, Hrd};
   return tiled_entry(n, nl, nr, L, nq, blk, npts, E, qidx, zero_flag, eta, eta0, dev_factor, convergence, max_iter,
-                     arith, &c, transl, status, iters, work, work_bytes, stream);
+                     arith, circ_on ? &c : nullptr, transl, transr, status, iters, work, work_bytes, stream);
 }
 
 }  // extern "C"

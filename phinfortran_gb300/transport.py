@@ -105,10 +105,9 @@ def _transport_tiled(E, nq, dims, arrs, *, eta, eta0, convergence, dev_factor, q
     products), "tc" (the FP64 algorithm with every block product on the
     tensor cores as exact BF16 slice products), "df64" (double-float
     arithmetic on the FP32 pipe, ~48-bit); "mixed" selects "tc".
-    circular: block-circulant leads (pf_transport_tdb_tiled_circ_dev)."""
+    circular: block-circulant leads; want_transr: T_R from the right-to-left
+    sweep as well (both through pf_transport_tdb_tiled_ex_dev)."""
     import torch
-    if want_transr:
-        raise ValueError("T_R is not computed for blocks above 48 (pass want_transr=False)")
     arith = TILED_ARITH[precision]
     lib = _abi.load()
     n, nl, nr, L = dims
@@ -119,6 +118,7 @@ def _transport_tiled(E, nq, dims, arrs, *, eta, eta0, convergence, dev_factor, q
     qd = None if qidx is None else torch.from_numpy(np.ascontiguousarray(qidx, dtype=np.int32)).cuda()
     zd = None if zero_flag is None else torch.from_numpy(np.ascontiguousarray(zero_flag, dtype=np.int32)).cuda()
     tl = torch.zeros(max(npts, 1), dtype=torch.float64, device="cuda")
+    trr = torch.zeros(max(npts, 1), dtype=torch.float64, device="cuda") if want_transr else None
     st = torch.zeros(max(npts, 1), dtype=torch.int32, device="cuda")
     it = torch.zeros((max(npts, 1), 2), dtype=torch.int32, device="cuda")
     p = lambda t: None if t is None else t.data_ptr()
@@ -126,26 +126,29 @@ def _transport_tiled(E, nq, dims, arrs, *, eta, eta0, convergence, dev_factor, q
     head = (n, nl, nr, L, nq, *[dev[k].data_ptr() for k in BLOCK_NAMES], npts, Ed.data_ptr(), p(qd), p(zd), eta,
             eta0, dev_factor, convergence, max_iter, arith)
     outs = (tl.data_ptr(), st.data_ptr(), it.data_ptr())
-    if circular is None:
+    if circular is None and not want_transr:
         ws = lib.pf_transport_tdb_tiled_workspace_size(n, nl, nr, L, nq, npts, arith)
         if ws == 0:
             _abi.check(-3)
         work = torch.empty(ws, dtype=torch.uint8, device="cuda")
         rc = lib.pf_transport_tdb_tiled_dev(*head, *outs, work.data_ptr(), ws, stream)
     else:
-        ny, nx, gr = _circular_args(circular, nl, nr)
-        ws = lib.pf_transport_tdb_tiled_circ_workspace_size(n, nl, nr, L, nq, npts, arith, ny, nx)
+        # pf_transport_tdb_tiled_ex_dev: block-circulant leads and / or T_R
+        ny, nx, gr = _circular_args(circular, nl, nr) if circular is not None else (1, 1, None)
+        ws = lib.pf_transport_tdb_tiled_ex_workspace_size(n, nl, nr, L, nq, npts, arith, ny, nx)
         if ws == 0:
             _abi.check(-3)
         work = torch.empty(ws, dtype=torch.uint8, device="cuda")
-        rc = lib.pf_transport_tdb_tiled_circ_dev(*head, ny, nx, _ptr(gr), *outs, work.data_ptr(), ws, stream)
+        rc = lib.pf_transport_tdb_tiled_ex_dev(*head, ny, nx, None if gr is None else _ptr(gr), tl.data_ptr(),
+                                               p(trr), st.data_ptr(), it.data_ptr(), work.data_ptr(), ws, stream)
     if rc != 0:
         raise _abi.PFError(rc, lib.pf_tiled_last_error().decode(errors="replace"))
     torch.cuda.synchronize()
     status = st.cpu().numpy()[:npts]
     if check and (status != 0).any():
         raise _abi.PFError(-4, f"point status flags 0x{int(np.bitwise_or.reduce(status)):x}")
-    return dict(transl=tl.cpu().numpy()[:npts], transr=None, status=status, iters=it.cpu().numpy()[:npts])
+    return dict(transl=tl.cpu().numpy()[:npts], transr=None if trr is None else trr.cpu().numpy()[:npts],
+                status=status, iters=it.cpu().numpy()[:npts])
 
 
 def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=None,
@@ -168,7 +171,9 @@ def transport_tdb(E, blocks, *, eta, eta0, convergence, dev_factor=10.0, qidx=No
     (n_bloch_y, n_bloch_x, gr) or a dict with those keys, gr = the G.R
     products {left y, left x, right y, right x}; the lead surface Green's
     functions then come from circular_g (negf/circular.f90:42-105) on the
-    large-block engine, at any block size, with T_L only.
+    large-block engine, at any block size.  On the large-block engine
+    want_transr adds the right-to-left sweep and T_R (off in "mixed" below
+    48, which computes T_L only).
     Returns dict(transl, transr, status, iters).
     """
     if precision not in TILED_ARITH:

@@ -120,3 +120,16 @@ def test_circular_rejects_bad_cells(cuda_ready, fx):
     b = {k: np.asarray(v) for k, v in sisi_blocks(fx, 0).items()}
     with pytest.raises(ValueError):
         transport_tdb(np.array([0.1]), b, want_transr=False, circular=(5, 2, [TWO_PI] * 4), **p)
+
+
+def test_circular_transr(cuda_ready, fx):
+    """T_R with block-circulant leads: the right-to-left sweep after the
+    circular surface functions, against the oracle's direct T_R."""
+    p = sisi_params(fx)
+    b = {k: np.asarray(v) for k, v in sisi_blocks(fx, 24).items()}
+    E = np.asarray(fx["E"][3:60:9], dtype=np.float64)
+    r = transport_tdb(E, b, want_transr=True, circular=(2, 2, _sisi_gr(fx)), **p)
+    assert (r["status"] == 0).all()
+    o = N.transport(E, b, p["eta"], p["eta0"], p["convergence"], p["dev_factor"])
+    assert _rel(r["transr"], o["transr"]).max() < 1e-9
+    assert _rel(r["transl"], o["transl"]).max() < 1e-9

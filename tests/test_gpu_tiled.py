@@ -109,3 +109,30 @@ def test_tiled_tensor_core(cuda_ready, case):
         b, E, p, aux = S.diamond_phonon(nc=3, L=3, nk_side=8, ne=12, kpoints=[9], block=2)
         bq = {k: v[0] for k, v in b.items()}
         check_against_oracle(bq, E[3:9:2], p, precision="tc")
+
+
+@pytest.mark.parametrize("system,precision", [("bar", "fp64"), ("bar", "tc"), ("diamond", "fp64"),
+                                              ("diamond", "tc")])
+def test_tiled_transr(cuda_ready, system, precision):
+    """want_transr on the large-block engine (pf_transport_tdb_tiled_ex_dev):
+    the right-to-left sweep and T_R (negf/lesser.f90:694-800) against the
+    oracle's, on a disordered bar (n = 108, identical leads: the right
+    surface function mirrored from the left) and on a diamond slab with a
+    mass interface (n = 96, leads of different mass: both decimated), and
+    T_L unchanged by the option."""
+    if system == "bar":
+        b, E, p, _ = S.sc_phonon(nx=6, ny=6, L=5, ne=16, seed_index=15, lead_mass=1.3)
+        E = E[1:]
+    else:
+        bq, E, p, _ = S.diamond_phonon(nc=2, L=6, nk_side=1, ne=16, block=3)
+        b = {k: v[0] for k, v in bq.items()}
+        E = E[1::2]
+        assert not np.array_equal(b["HL"], b["HR"])
+    r = transport_tdb(E, b, want_transr=True, precision=precision, **p)
+    assert (r["status"] == 0).all()
+    o = N.transport(E, b, p["eta"], p["eta0"], p["convergence"], p["dev_factor"])
+    rel = lambda a, c: np.abs(a - c) / np.maximum(np.abs(c), 1.0)
+    assert rel(r["transr"], o["transr"]).max() < 1e-9
+    assert rel(r["transl"], o["transl"]).max() < 1e-9
+    r0 = transport_tdb(E, b, want_transr=False, precision=precision, **p)
+    assert np.array_equal(r0["transl"], r["transl"])
