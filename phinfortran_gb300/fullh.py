@@ -311,9 +311,15 @@ class FullH:
         return dev, (n, nl, nr, L, nq)
 
     def transport(self, E, kfrac, qidx=None, *, eta, eta0, convergence, dev_factor=10.0, max_iter=1000,
-                  precision="fp64", refine_iters=2):
+                  precision="fp64", refine_iters=2, want_transr=False):
         """T_L of every point (E[p] at k = kfrac[qidx[p]]): D(q) built and
-        sliced on the GPU, then the tdb transport engine on device blocks."""
+        sliced on the GPU, then the tdb transport engine on device blocks.
+        want_transr (FP64 and the large-block arithmetics) adds T_R from the
+        right-to-left sweep of G_block (negf/device.f90:289-560) as transr,
+        without the reference's debug override of G_NN near E = 31.2954
+        (device.f90:485-493)."""
+        if want_transr and precision == "mixed":
+            raise ValueError("the mixed path computes T_L only")
         from .transport import DeviceTransport
         torch = self.torch
         H = self.dynamical(kfrac)
@@ -325,14 +331,17 @@ class FullH:
             blocks = {k: np.swapaxes(v[..., 0].cpu().numpy() + 1j * v[..., 1].cpu().numpy(), -1, -2)
                       for k, v in dev.items()}
             return transport_tdb(E, blocks, eta=eta, eta0=eta0, convergence=convergence, dev_factor=dev_factor,
-                                 qidx=qidx, max_iter=max_iter, want_transr=False, check=False,
+                                 qidx=qidx, max_iter=max_iter, want_transr=want_transr, check=False,
                                  precision=precision)
         tr = DeviceTransport.from_device({k: v.reshape(-1) for k, v in dev.items()}, dims, E.size, eta=eta,
                                          eta0=eta0, convergence=convergence, dev_factor=dev_factor,
                                          max_iter=max_iter, precision=precision, refine_iters=refine_iters,
-                                         device=self.device)
+                                         device=self.device, want_transr=want_transr)
         Ed = torch.from_numpy(E).to(self.device)
         qd = None if qidx is None else torch.from_numpy(np.ascontiguousarray(qidx, dtype=np.int32)).to(self.device)
-        tl, _, st = tr.run(Ed, qd)
+        tl, trr, st = tr.run(Ed, qd)
         torch.cuda.synchronize()
-        return dict(transl=tl.cpu().numpy().copy(), status=st.cpu().numpy().copy())
+        out = dict(transl=tl.cpu().numpy().copy(), status=st.cpu().numpy().copy())
+        if want_transr:
+            out["transr"] = trr.cpu().numpy().copy()
+        return out

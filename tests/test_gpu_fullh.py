@@ -90,12 +90,15 @@ def test_slices_and_transmission(case):
     E = np.tile(Es, nq)
     qidx = np.repeat(np.arange(nq, dtype=np.int32), Es.size)
     p = dict(eta=1e-6, eta0=0.0, convergence=1e-12, dev_factor=10.0)
-    got = F.transport(E, KPTS, qidx, **p)
+    got = F.transport(E, KPTS, qidx, want_transr=True, **p)
     assert not got["status"].any()
     for q in range(nq):
         B = O.dense_to_tdb(case["H_oracle"][q], ll, nl, nr, case["n_buffer_l"], case["n_buffer_r"])
-        ref = N.transport(Es, B, **p)["transl"]
+        o = N.transport(Es, B, **p)
+        ref = o["transl"]
         assert np.allclose(got["transl"][q * Es.size:(q + 1) * Es.size], ref, rtol=1e-9, atol=1e-12), q
+        # T_R from the right-to-left sweep of G_block (device.f90:289-560)
+        assert np.allclose(got["transr"][q * Es.size:(q + 1) * Es.size], o["transr"], rtol=1e-9, atol=1e-12), q
     # at the zone centre the chain is the bar of the tdb workloads
     bar_T = N.transport(Es, case["bar_blocks"], **p)["transl"]
     assert np.allclose(got["transl"][:Es.size], bar_T, rtol=1e-9, atol=1e-12)
