@@ -306,6 +306,53 @@ def circular_sample(torch, nc=3, ne=64):
                 note="host-pointer call, tensor-core products; deviation = max |T_circ - T_full| / max(|T_full|, 1e-3)")
 
 
+def tc_zgemm_rate(torch, m=384, batch=64, reps=5):
+    """The batched tensor-core ZGEMM of the large-block engine
+    (pf_tc_zgemm_dev, FP64-grade: 9 BF16 slices an operand, the 45 slice
+    pairs with s + t <= 10, each a real GEMM of 8 m n k flops on the
+    interleaved embedding) on m = n = k, batch products, inputs of 3 x 151 MB
+    (above L2).  CUDA events around each call on its stream (slicing,
+    exponent scans, products and assembly), after 3 warm-up calls."""
+    import ctypes as C
+    from phinfortran_gb300 import _abi
+    lib = _abi.load()
+    g = torch.Generator(device="cuda").manual_seed(5)
+    A = torch.randn(batch * m * m * 2, dtype=torch.float64, device="cuda", generator=g)
+    B = torch.randn(batch * m * m * 2, dtype=torch.float64, device="cuda", generator=g)
+    Cm = torch.zeros(batch * m * m * 2, dtype=torch.float64, device="cuda")
+    ws = lib.pf_tc_zgemm_workspace_size(m, m, m, batch, 0, 0)
+    work = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream()
+    s2 = m * m
+
+    def call():
+        rc = lib.pf_tc_zgemm_dev(ord("N"), ord("N"), m, m, m, 1.0, A.data_ptr(), m, s2, B.data_ptr(), m, s2, 0.0,
+                                 Cm.data_ptr(), m, s2, batch, work.data_ptr(), ws, C.c_void_p(st.cuda_stream))
+        if rc != 0:
+            raise _abi.PFError(rc, lib.pf_tc_last_error().decode(errors="replace"))
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        call()
+        e1.record(st)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    t = statistics.median(times)
+    fl = 8.0 * m * m * m * batch
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
+    bf16 = 45 * fl / t / 1e12
+    return dict(m=m, n=m, k=m, batch=batch, ms_per_call=t * 1e3, fp64_equivalent_tflops=fl / t / 1e12,
+                bf16_tensor_tflops=bf16, bf16_peak_tflops=bf16_peak, frac_of_bf16_peak=bf16 / bf16_peak,
+                slice_pairs=45, note="whole call (slicing + products + FP64 assembly); bf16 = 45 pair products x "
+                                     "8 m n k flops a product; peak: dense bf16 burst of MEASURED_PEAKS.json")
+
+
 def gradient_ratio(torch, flush, stream, steps):
     """Adjoint gradient (d kappa / d every block) vs one forward sweep on the
     simple-cubic 4x4x40 bar (n=48, L=40), masses U[1,3], springs U[0.8,1.2],
@@ -516,8 +563,10 @@ def main():
 
     # ---- large blocks: diamond slab stacks (n = 96, 216; L = 60) ----
     large = None
+    tcz = None
     if not args.no_large:
         large = large_block_sample(torch)
+        tcz = tc_zgemm_rate(torch)
 
     # ---- end to end through the host-pointer C entry ----
     nq, dims, arrs = TdbBlocks.from_dict(b).stacked()
@@ -636,7 +685,7 @@ def main():
                 direct_launch_ms_per_step=None if t_direct is None else t_direct * 1e3,
                 e2e=dict(value=e2e_value, unit="solves/s", h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h),
                          entry="pf_transport_tdb_mixed" if args.path == "mixed" else "pf_transport_tdb"),
-                roofline=roof, cpu_baseline=cpu, compare=compare, gradient=grad, large_blocks=large,
+                roofline=roof, cpu_baseline=cpu, compare=compare, gradient=grad, large_blocks=large, tc_zgemm=tcz,
                 clocks=dict(sm_mhz=clk["sm_mhz"], sm_max_mhz=clk["sm_max_mhz"], reasons=clk["reasons"]),
                 gpu_launches=launches_per_step * args.steps, status_nonzero=int((status != 0).sum()))
     print(json.dumps(line), flush=True)
